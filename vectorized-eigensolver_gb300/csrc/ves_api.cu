@@ -1,0 +1,513 @@
+// ves_api.cu -- the C ABI of libves.so (declared in include/ves.h).
+//
+// Drop-in layer: the reference's host entry points (utils.cpp) with host
+// pointers and synchronous semantics.  Each call copies its inputs to device
+// buffers that the library caches between calls (the reference allocates and
+// frees them in every call, utils.cpp:178-214), runs the sm_103a kernels and
+// copies the results back.
+//
+// Native layer: ves_* on device pointers, stream-ordered.
+#include "ves.h"
+#include "ves_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace {
+
+constexpr int kMaxDim = 512;
+
+thread_local std::string t_last_error;
+
+void set_error(const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    t_last_error = buf;
+}
+
+// Drop-in layer failures go to stderr as well: the reference API returns void.
+void report(const char *where)
+{
+    fprintf(stderr, "libves: %s: %s\n", where, t_last_error.c_str());
+}
+
+bool cuda_ok(cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return true;
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return false;
+}
+
+bool geom_ok(int dim, int block_cnt, int thread_cnt, ves::Geom *g)
+{
+    if (dim < 1 || dim > kMaxDim) { set_error("dim=%d outside [1, %d]", dim, kMaxDim); return false; }
+    if (block_cnt < 0 || thread_cnt < 1) {
+        set_error("block_cnt=%d thread_cnt=%d: need block_cnt >= 0, thread_cnt >= 1", block_cnt, thread_cnt);
+        return false;
+    }
+    g->n = dim;
+    g->N = (long long)block_cnt * thread_cnt;
+    g->tc = thread_cnt;
+    return true;
+}
+
+// Grow-only device buffers, one set per device, shared by the drop-in calls
+// (serialised by a mutex).
+struct Pool {
+    std::mutex mu;
+    struct Slot { void *p = nullptr; size_t n = 0; };
+    std::vector<std::vector<Slot>> dev;  // [device][slot]
+
+    void *get(int slot, size_t bytes)
+    {
+        int d = 0;
+        if (cudaGetDevice(&d) != cudaSuccess) return nullptr;
+        if ((int)dev.size() <= d) dev.resize(d + 1);
+        if ((int)dev[d].size() <= slot) dev[d].resize(slot + 1);
+        Slot &s = dev[d][slot];
+        if (bytes == 0) bytes = 1;
+        if (s.n >= bytes) return s.p;
+        if (s.p) cudaFree(s.p);
+        s.p = nullptr;
+        s.n = 0;
+        if (cudaMalloc(&s.p, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            s.p = nullptr;
+            return nullptr;
+        }
+        s.n = bytes;
+        return s.p;
+    }
+    void release()
+    {
+        int cur = 0;
+        cudaGetDevice(&cur);
+        for (size_t d = 0; d < dev.size(); ++d) {
+            if (cudaSetDevice((int)d) != cudaSuccess) continue;
+            for (Slot &s : dev[d])
+                if (s.p) cudaFree(s.p);
+            dev[d].clear();
+        }
+        cudaSetDevice(cur);
+    }
+};
+Pool &pool()
+{
+    static Pool *p = new Pool();  // never destroyed: freeing at exit races the CUDA runtime's teardown
+    return *p;
+}
+
+// Scoped acquisition of the pool for one drop-in call.
+struct Bufs {
+    std::lock_guard<std::mutex> lk;
+    Bufs() : lk(pool().mu) {}
+    double *d(int slot, size_t count) { return static_cast<double *>(pool().get(slot, count * sizeof(double))); }
+    void *raw(int slot, size_t bytes) { return pool().get(slot, bytes); }
+};
+
+bool h2d(void *dst, const void *src, size_t bytes) { return cuda_ok(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice), "cudaMemcpy H2D"); }
+bool d2h(void *dst, const void *src, size_t bytes) { return cuda_ok(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost), "cudaMemcpy D2H"); }
+bool sync_ok(const char *what) { return cuda_ok(cudaDeviceSynchronize(), what); }
+
+#define NEED(ptr)                                                    \
+    do {                                                             \
+        if (!(ptr)) { set_error("device allocation failed"); return false; } \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// Drop-in bodies (bool: success).
+// ---------------------------------------------------------------------------
+bool do_eigensolver(int dim, int bc, int tc, double *rA, double *iA, double *rE, double *iE, double *rV, double *iV)
+{
+    ves::Geom g;
+    if (!geom_ok(dim, bc, tc, &g)) return false;
+    if (g.N == 0) return true;
+    if (!rA || !iA || !rE || !iE || !rV || !iV) { set_error("null pointer"); return false; }
+    const size_t nm = (size_t)g.N * dim * dim, nv = (size_t)g.N * dim;
+    Bufs b;
+    double *dAr = b.d(0, nm), *dAi = b.d(1, nm), *dVr = b.d(2, nm), *dVi = b.d(3, nm);
+    double *dEr = b.d(4, nv), *dEi = b.d(5, nv);
+    NEED(dAr); NEED(dAi); NEED(dVr); NEED(dVi); NEED(dEr); NEED(dEi);
+    const size_t wsb = ves::fused_workspace_bytes(dim, g.N, nullptr, nullptr);
+    void *ws = b.raw(6, wsb);
+    NEED(ws);
+    if (!h2d(dAr, rA, nm * 8) || !h2d(dAi, iA, nm * 8)) return false;
+    ves::FusedArgs a{};
+    a.g = g;
+    a.rA = dAr; a.iA = dAi;
+    a.rE = dEr; a.iE = dEi;
+    a.rV = dVr; a.iV = dVi;
+    a.rT = dAr; a.iT = dAi;  // A is overwritten with T, as in the reference
+    a.ws = ws;
+    a.max_its = 30;
+    a.vnorm = VES_VNORM_REFERENCE;
+    if (!cuda_ok(ves::launch_fused_fp64(a, 0), "eigensolver kernel launch")) return false;
+    if (!sync_ok("eigensolver kernel")) return false;
+    return d2h(rA, dAr, nm * 8) && d2h(iA, dAi, nm * 8) && d2h(rE, dEr, nv * 8) && d2h(iE, dEi, nv * 8) &&
+           d2h(rV, dVr, nm * 8) && d2h(iV, dVi, nm * 8);
+}
+
+bool do_hessenberg(int dim, int bc, int tc, double *rA, double *iA, double *rQ, double *iQ)
+{
+    ves::Geom g;
+    if (!geom_ok(dim, bc, tc, &g)) return false;
+    if (g.N == 0) return true;
+    if (!rA || !iA || !rQ || !iQ) { set_error("null pointer"); return false; }
+    const size_t nm = (size_t)g.N * dim * dim, nv = (size_t)g.N * dim;
+    Bufs b;
+    double *dAr = b.d(0, nm), *dAi = b.d(1, nm), *dQr = b.d(2, nm), *dQi = b.d(3, nm);
+    double *dtr = b.d(4, nv), *dti = b.d(5, nv);
+    NEED(dAr); NEED(dAi); NEED(dQr); NEED(dQi); NEED(dtr); NEED(dti);
+    if (!h2d(dAr, rA, nm * 8) || !h2d(dAi, iA, nm * 8)) return false;
+    if (!cuda_ok(ves::launch_hessenberg(g, dAr, dAi, dQr, dQi, dtr, dti, 0), "hessenberg kernel launch")) return false;
+    if (!sync_ok("hessenberg kernel")) return false;
+    return d2h(rA, dAr, nm * 8) && d2h(iA, dAi, nm * 8) && d2h(rQ, dQr, nm * 8) && d2h(iQ, dQi, nm * 8);
+}
+
+bool do_zgehrd(int dim, int bc, int tc, double *rA, double *iA, double *rtau, double *itau)
+{
+    ves::Geom g;
+    if (!geom_ok(dim, bc, tc, &g)) return false;
+    if (g.N == 0) return true;
+    if (!rA || !iA || !rtau || !itau) { set_error("null pointer"); return false; }
+    const size_t nm = (size_t)g.N * dim * dim, nv = (size_t)g.N * dim;
+    Bufs b;
+    double *dAr = b.d(0, nm), *dAi = b.d(1, nm), *dtr = b.d(4, nv), *dti = b.d(5, nv);
+    NEED(dAr); NEED(dAi); NEED(dtr); NEED(dti);
+    if (!h2d(dAr, rA, nm * 8) || !h2d(dAi, iA, nm * 8)) return false;
+    // tau's last entry per matrix is not written by the reduction: keep the caller's values there
+    if (!h2d(dtr, rtau, nv * 8) || !h2d(dti, itau, nv * 8)) return false;
+    if (!cuda_ok(ves::launch_zgehrd(g, dAr, dAi, dtr, dti, 0), "zgehrd kernel launch")) return false;
+    if (!sync_ok("zgehrd kernel")) return false;
+    return d2h(rA, dAr, nm * 8) && d2h(iA, dAi, nm * 8) && d2h(rtau, dtr, nv * 8) && d2h(itau, dti, nv * 8);
+}
+
+bool do_zunghr(int dim, int bc, int tc, double *rA, double *iA, double *rtau, double *itau)
+{
+    ves::Geom g;
+    if (!geom_ok(dim, bc, tc, &g)) return false;
+    if (g.N == 0) return true;
+    if (!rA || !iA || !rtau || !itau) { set_error("null pointer"); return false; }
+    const size_t nm = (size_t)g.N * dim * dim, nv = (size_t)g.N * dim;
+    Bufs b;
+    double *dAr = b.d(0, nm), *dAi = b.d(1, nm), *dtr = b.d(4, nv), *dti = b.d(5, nv);
+    NEED(dAr); NEED(dAi); NEED(dtr); NEED(dti);
+    if (!h2d(dAr, rA, nm * 8) || !h2d(dAi, iA, nm * 8) || !h2d(dtr, rtau, nv * 8) || !h2d(dti, itau, nv * 8))
+        return false;
+    if (!cuda_ok(ves::launch_zunghr(g, dAr, dAi, dtr, dti, 0), "zunghr kernel launch")) return false;
+    if (!sync_ok("zunghr kernel")) return false;
+    return d2h(rA, dAr, nm * 8) && d2h(iA, dAi, nm * 8);
+}
+
+bool do_zlahqr(int dim, int bc, int tc, double *rE, double *iE, double *rM, double *iM, double *rS, double *iS)
+{
+    ves::Geom g;
+    if (!geom_ok(dim, bc, tc, &g)) return false;
+    if (g.N == 0) return true;
+    if (!rE || !iE || !rM || !iM || !rS || !iS) { set_error("null pointer"); return false; }
+    const size_t nm = (size_t)g.N * dim * dim, nv = (size_t)g.N * dim;
+    Bufs b;
+    double *dMr = b.d(0, nm), *dMi = b.d(1, nm), *dSr = b.d(2, nm), *dSi = b.d(3, nm);
+    double *dEr = b.d(4, nv), *dEi = b.d(5, nv);
+    NEED(dMr); NEED(dMi); NEED(dSr); NEED(dSi); NEED(dEr); NEED(dEi);
+    if (!h2d(dMr, rM, nm * 8) || !h2d(dMi, iM, nm * 8)) return false;
+    if (!cuda_ok(ves::launch_zlahqr(g, dEr, dEi, dMr, dMi, dSr, dSi, nullptr, 30, 0), "zlahqr kernel launch"))
+        return false;
+    if (!sync_ok("zlahqr kernel")) return false;
+    return d2h(rE, dEr, nv * 8) && d2h(iE, dEi, nv * 8) && d2h(rM, dMr, nm * 8) && d2h(iM, dMi, nm * 8) &&
+           d2h(rS, dSr, nm * 8) && d2h(iS, dSi, nm * 8);
+}
+
+bool do_ztrevc(int dim, int bc, int tc, double *rT, double *iT, double *rR, double *iR)
+{
+    ves::Geom g;
+    if (!geom_ok(dim, bc, tc, &g)) return false;
+    if (g.N == 0) return true;
+    if (!rT || !iT || !rR || !iR) { set_error("null pointer"); return false; }
+    const size_t nm = (size_t)g.N * dim * dim, nv = (size_t)g.N * dim;
+    Bufs b;
+    double *dTr = b.d(0, nm), *dTi = b.d(1, nm), *dRr = b.d(2, nm), *dRi = b.d(3, nm);
+    double *dwr = b.d(4, nv), *dwi = b.d(5, nv);
+    NEED(dTr); NEED(dTi); NEED(dRr); NEED(dRi); NEED(dwr); NEED(dwi);
+    if (!h2d(dTr, rT, nm * 8) || !h2d(dTi, iT, nm * 8) || !h2d(dRr, rR, nm * 8) || !h2d(dRi, iR, nm * 8))
+        return false;
+    if (!cuda_ok(ves::launch_ztrevc(g, dTr, dTi, dRr, dRi, dwr, dwi, 0), "ztrevc kernel launch")) return false;
+    if (!sync_ok("ztrevc kernel")) return false;
+    return d2h(rR, dRr, nm * 8) && d2h(iR, dRi, nm * 8);
+}
+
+bool do_zgemv(bool herm, int dim, int bc, int tc, double *rM, double *iM, double *rx, double *ix, double *ry,
+              double *iy, double rbeta, double ibeta)
+{
+    ves::Geom g;
+    if (!geom_ok(dim, bc, tc, &g)) return false;
+    if (g.N == 0) return true;
+    if (!rM || !iM || !rx || !ix || !ry || !iy) { set_error("null pointer"); return false; }
+    const size_t nm = (size_t)g.N * dim * dim, nv = (size_t)g.N * dim;
+    Bufs b;
+    double *dMr = b.d(0, nm), *dMi = b.d(1, nm), *dxr = b.d(4, nv), *dxi = b.d(5, nv);
+    double *dyr = b.d(7, nv), *dyi = b.d(8, nv);
+    NEED(dMr); NEED(dMi); NEED(dxr); NEED(dxi); NEED(dyr); NEED(dyi);
+    if (!h2d(dMr, rM, nm * 8) || !h2d(dMi, iM, nm * 8) || !h2d(dxr, rx, nv * 8) || !h2d(dxi, ix, nv * 8) ||
+        !h2d(dyr, ry, nv * 8) || !h2d(dyi, iy, nv * 8))
+        return false;
+    if (!cuda_ok(ves::launch_zgemv(g, herm, dMr, dMi, dxr, dxi, rbeta, ibeta, dyr, dyi, 0), "zgemv kernel launch"))
+        return false;
+    if (!sync_ok("zgemv kernel")) return false;
+    return d2h(ry, dyr, nv * 8) && d2h(iy, dyi, nv * 8);
+}
+
+bool do_backsubs(int dim, int bc, int tc, double *rT, double *iT, double *rb, double *ib)
+{
+    ves::Geom g;
+    if (!geom_ok(dim, bc, tc, &g)) return false;
+    if (g.N == 0) return true;
+    if (!rT || !iT || !rb || !ib) { set_error("null pointer"); return false; }
+    const size_t nm = (size_t)g.N * dim * dim, nv = (size_t)g.N * dim;
+    Bufs b;
+    double *dTr = b.d(0, nm), *dTi = b.d(1, nm), *dbr = b.d(4, nv), *dbi = b.d(5, nv);
+    NEED(dTr); NEED(dTi); NEED(dbr); NEED(dbi);
+    if (!h2d(dTr, rT, nm * 8) || !h2d(dTi, iT, nm * 8) || !h2d(dbr, rb, nv * 8) || !h2d(dbi, ib, nv * 8))
+        return false;
+    if (!cuda_ok(ves::launch_backsubs(g, dTr, dTi, dbr, dbi, 0), "backsubstitution kernel launch")) return false;
+    if (!sync_ok("backsubstitution kernel")) return false;
+    return d2h(rb, dbr, nv * 8) && d2h(ib, dbi, nv * 8);
+}
+
+template <class F>
+void dropin(const char *name, F f)
+{
+    t_last_error.clear();
+    if (!f()) report(name);
+}
+
+int native(bool ok) { return ok ? VES_OK : (t_last_error.find("alloc") != std::string::npos ? VES_ERR_NOMEM : VES_ERR_CUDA); }
+
+}  // namespace
+
+extern "C" {
+
+// ------------------------------- drop-in ----------------------------------
+void eigensolver(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rE, double *iE, double *rV,
+                 double *iV)
+{
+    dropin("eigensolver", [&] { return do_eigensolver(dim, block_cnt, thread_cnt, rA, iA, rE, iE, rV, iV); });
+}
+
+void hessenberg(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rQ, double *iQ)
+{
+    dropin("hessenberg", [&] { return do_hessenberg(dim, block_cnt, thread_cnt, rA, iA, rQ, iQ); });
+}
+
+void call_zgehrd(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau)
+{
+    dropin("call_zgehrd", [&] { return do_zgehrd(dim, block_cnt, thread_cnt, rA, iA, rtau, itau); });
+}
+
+void call_zunghr(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau)
+{
+    dropin("call_zunghr", [&] { return do_zunghr(dim, block_cnt, thread_cnt, rA, iA, rtau, itau); });
+}
+
+void call_zlahqr_new(int dim, int block_cnt, int thread_cnt, double *rE, double *iE, double *rM, double *iM, double *rS,
+                     double *iS)
+{
+    dropin("call_zlahqr_new", [&] { return do_zlahqr(dim, block_cnt, thread_cnt, rE, iE, rM, iM, rS, iS); });
+}
+
+void call_ztrevc(int dim, int block_cnt, int thread_cnt, double *rT, double *iT, double *rR, double *iR)
+{
+    dropin("call_ztrevc", [&] { return do_ztrevc(dim, block_cnt, thread_cnt, rT, iT, rR, iR); });
+}
+
+void call_zgemv(bool hermitian, int dim, int block_cnt, int thread_cnt, double *rM, double *iM, double *rx, double *ix,
+                double *ry, double *iy, double rbeta, double ibeta)
+{
+    dropin("call_zgemv", [&] {
+        return do_zgemv(hermitian, dim, block_cnt, thread_cnt, rM, iM, rx, ix, ry, iy, rbeta, ibeta);
+    });
+}
+
+void call_backsubstitution(int dim, int block_cnt, int thread_cnt, double *rT, double *iT, double *rb, double *ib)
+{
+    dropin("call_backsubstitution", [&] { return do_backsubs(dim, block_cnt, thread_cnt, rT, iT, rb, ib); });
+}
+
+void repMatrixSoA(int dim, int block_cnt, int thread_cnt, double *matrix, double *out)
+{
+    const long long n2 = (long long)dim * dim;
+    for (long long e = 0; e < n2; ++e)
+        for (long long b = 0; b < block_cnt; ++b)
+            for (long long t = 0; t < thread_cnt; ++t) out[b * thread_cnt * n2 + e * thread_cnt + t] = matrix[e];
+}
+
+void repVectorSoA(int dim, int block_cnt, int thread_cnt, double *vec, double *out)
+{
+    for (long long e = 0; e < dim; ++e)
+        for (long long b = 0; b < block_cnt; ++b)
+            for (long long t = 0; t < thread_cnt; ++t) out[b * thread_cnt * dim + e * thread_cnt + t] = vec[e];
+}
+
+void rearrangeMatrices(int dim, int block_cnt, int thread_cnt, double *in, double *out)
+{
+    const long long n2 = (long long)dim * dim;
+    for (long long b = 0; b < block_cnt; ++b)
+        for (long long t = 0; t < thread_cnt; ++t)
+            for (long long e = 0; e < n2; ++e)
+                out[b * thread_cnt * n2 + e * thread_cnt + t] = in[(b * thread_cnt + t) * n2 + e];
+}
+
+void arrangeMatricesAoS(int dim, int block_cnt, int thread_cnt, double *in, double *out)
+{
+    const long long n2 = (long long)dim * dim;
+    for (long long b = 0; b < block_cnt; ++b)
+        for (long long t = 0; t < thread_cnt; ++t)
+            for (long long e = 0; e < n2; ++e)
+                out[(b * thread_cnt + t) * n2 + e] = in[b * thread_cnt * n2 + e * thread_cnt + t];
+}
+
+// -------------------------------- native ----------------------------------
+void ves_default_options(ves_options *opt)
+{
+    if (!opt) return;
+    memset(opt, 0, sizeof *opt);
+    opt->precision = VES_PREC_FP64;
+    opt->max_its = 30;
+    opt->vnorm = VES_VNORM_REFERENCE;
+}
+
+size_t ves_eigensolve_workspace_size(int dim, int block_cnt, int thread_cnt, const ves_options *opt)
+{
+    (void)opt;
+    ves::Geom g;
+    if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return 0;
+    return ves::fused_workspace_bytes(dim, g.N, nullptr, nullptr);
+}
+
+int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, const double *iA, double *rE, double *iE,
+                   double *rV, double *iV, double *rT, double *iT, int *status, int *sweeps, const ves_options *opt,
+                   void *workspace, size_t workspace_bytes, void *stream)
+{
+    t_last_error.clear();
+    ves::Geom g;
+    if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
+    if (g.N == 0) return VES_OK;
+    if (!rA || !iA || !rE || !iE || !rV || !iV || (!rT) != (!iT)) { set_error("null pointer"); return VES_ERR_ARG; }
+    ves_options o;
+    ves_default_options(&o);
+    if (opt) o = *opt;
+    if (o.precision != VES_PREC_FP64) { set_error("precision mode %d not available", o.precision); return VES_ERR_UNSUPPORTED; }
+    if (o.max_its < 0 || o.max_its > 10000) { set_error("max_its=%d outside [0, 10000]", o.max_its); return VES_ERR_ARG; }
+    if (o.vnorm < 0 || o.vnorm > 2) { set_error("vnorm=%d unknown", o.vnorm); return VES_ERR_ARG; }
+    const size_t need = ves::fused_workspace_bytes(dim, g.N, nullptr, nullptr);
+    void *ws = workspace;
+    std::unique_lock<std::mutex> lk;
+    if (!ws) {
+        lk = std::unique_lock<std::mutex>(pool().mu);
+        ws = pool().get(15, need);
+        if (!ws) { set_error("device allocation of %zu workspace bytes failed", need); return VES_ERR_NOMEM; }
+    } else if (workspace_bytes < need || ((uintptr_t)ws & 255)) {
+        set_error("workspace: %zu bytes given, %zu needed (256-byte aligned)", workspace_bytes, need);
+        return VES_ERR_ARG;
+    }
+    ves::FusedArgs a{};
+    a.g = g;
+    a.rA = rA; a.iA = iA;
+    a.rE = rE; a.iE = iE;
+    a.rV = rV; a.iV = iV;
+    a.rT = rT; a.iT = iT;
+    a.status = status; a.sweeps = sweeps;
+    a.ws = ws;
+    a.max_its = o.max_its;
+    a.vnorm = o.vnorm;
+    return native(cuda_ok(ves::launch_fused_fp64(a, (cudaStream_t)stream), "eigensolve kernel launch"));
+}
+
+int ves_zgehrd(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau, void *stream)
+{
+    t_last_error.clear();
+    ves::Geom g;
+    if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
+    return native(cuda_ok(ves::launch_zgehrd(g, rA, iA, rtau, itau, (cudaStream_t)stream), "zgehrd launch"));
+}
+
+int ves_zunghr(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, const double *rtau, const double *itau,
+               void *stream)
+{
+    t_last_error.clear();
+    ves::Geom g;
+    if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
+    return native(cuda_ok(ves::launch_zunghr(g, rA, iA, rtau, itau, (cudaStream_t)stream), "zunghr launch"));
+}
+
+int ves_hessenberg(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rQ, double *iQ,
+                   double *rtau, double *itau, void *stream)
+{
+    t_last_error.clear();
+    ves::Geom g;
+    if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
+    return native(cuda_ok(ves::launch_hessenberg(g, rA, iA, rQ, iQ, rtau, itau, (cudaStream_t)stream), "hessenberg launch"));
+}
+
+int ves_zlahqr(int dim, int block_cnt, int thread_cnt, double *rE, double *iE, double *rM, double *iM, double *rS,
+               double *iS, int *status, int max_its, void *stream)
+{
+    t_last_error.clear();
+    ves::Geom g;
+    if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
+    if (max_its < 0 || max_its > 10000) { set_error("max_its=%d outside [0, 10000]", max_its); return VES_ERR_ARG; }
+    return native(cuda_ok(ves::launch_zlahqr(g, rE, iE, rM, iM, rS, iS, status, max_its, (cudaStream_t)stream),
+                          "zlahqr launch"));
+}
+
+int ves_ztrevc(int dim, int block_cnt, int thread_cnt, double *rT, double *iT, double *rR, double *iR, double *rwork,
+               double *iwork, void *stream)
+{
+    t_last_error.clear();
+    ves::Geom g;
+    if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
+    return native(cuda_ok(ves::launch_ztrevc(g, rT, iT, rR, iR, rwork, iwork, (cudaStream_t)stream), "ztrevc launch"));
+}
+
+int ves_zgemv(bool hermitian, int dim, int block_cnt, int thread_cnt, const double *rM, const double *iM,
+              const double *rx, const double *ix, double *ry, double *iy, double rbeta, double ibeta, void *stream)
+{
+    t_last_error.clear();
+    ves::Geom g;
+    if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
+    return native(cuda_ok(ves::launch_zgemv(g, hermitian, rM, iM, rx, ix, rbeta, ibeta, ry, iy, (cudaStream_t)stream),
+                          "zgemv launch"));
+}
+
+int ves_backsubstitution(int dim, int block_cnt, int thread_cnt, const double *rT, const double *iT, double *rb,
+                         double *ib, void *stream)
+{
+    t_last_error.clear();
+    ves::Geom g;
+    if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
+    return native(cuda_ok(ves::launch_backsubs(g, rT, iT, rb, ib, (cudaStream_t)stream), "backsubstitution launch"));
+}
+
+const char *ves_last_error(void) { return t_last_error.c_str(); }
+
+void ves_release(void)
+{
+    std::lock_guard<std::mutex> lk(pool().mu);
+    pool().release();
+}
+
+int ves_version(void) { return 100; }
+
+}  // extern "C"

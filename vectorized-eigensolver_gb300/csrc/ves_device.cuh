@@ -1,0 +1,537 @@
+// ves_device.cuh -- per-matrix numerical routines of the batched eigensolver,
+// written for one matrix per CUDA lane with the 32 lanes of a warp in lockstep.
+//
+// Why one matrix per lane: on GB300 the FP64 pipe retires ~1.9 lane-FMAs per
+// clock per SM and a warp instruction occupies it for all 32 lanes whether or
+// not they are active.  Every FP64 warp instruction must therefore carry 32
+// useful operations: each lane owns one matrix, and all lanes run the same
+// instruction stream.  Data-dependent control flow (QR deflation) is handled
+// by keeping the K counter of a QR sweep warp-uniform while each lane keeps its
+// own active window [L, I], so addresses stay coalesced and only loop bounds
+// are predicated (zlahqr_warp below).
+//
+// Numerics follow the reference routines of kipfstuhl/vectorized-eigensolver
+// (Toolbox.hpp) and LAPACK, cited per routine; indices are 1-based through the
+// matrix accessors, as in both.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cfloat>
+#include <climits>
+
+namespace ves {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// status bits, one int per matrix
+constexpr int ST_ITCAP = 1;      // some eigenvalue hit the sweep cap (reference moves on silently)
+constexpr int ST_NONFINITE = 2;  // input held Inf/NaN
+constexpr int ST_SHIFT_FALLBACK = 4;  // learned shift abandoned for Wilkinson at least once
+constexpr int ST_REFINE_FALLBACK = 8; // mixed precision: pair did not converge, solved again in FP64
+
+template <class R> struct cx { R r, i; };
+
+template <class R> __device__ __forceinline__ cx<R> mk(R r, R i) { cx<R> z; z.r = r; z.i = i; return z; }
+template <class R> __device__ __forceinline__ R cabs1(cx<R> z) { return fabs(z.r) + fabs(z.i); }
+template <class R> __device__ __forceinline__ R cabs(cx<R> z) { return sqrt(z.r * z.r + z.i * z.i); }
+template <class R> __device__ __forceinline__ cx<R> cmul(cx<R> a, cx<R> b) { return mk(a.r * b.r - a.i * b.i, a.i * b.r + a.r * b.i); }
+// a * conj(b)
+template <class R> __device__ __forceinline__ cx<R> cmulc(cx<R> a, cx<R> b) { return mk(a.r * b.r + a.i * b.i, a.i * b.r - a.r * b.i); }
+// conj(a) * b
+template <class R> __device__ __forceinline__ cx<R> cjmul(cx<R> a, cx<R> b) { return mk(a.r * b.r + a.i * b.i, a.r * b.i - a.i * b.r); }
+template <class R> __device__ __forceinline__ cx<R> cadd(cx<R> a, cx<R> b) { return mk(a.r + b.r, a.i + b.i); }
+template <class R> __device__ __forceinline__ cx<R> csub(cx<R> a, cx<R> b) { return mk(a.r - b.r, a.i - b.i); }
+template <class R> __device__ __forceinline__ cx<R> cscal(cx<R> a, R d) { return mk(a.r * d, a.i * d); }
+template <class R> __device__ __forceinline__ cx<R> conj(cx<R> a) { return mk(a.r, -a.i); }
+
+// 1/z and a/b by Smith's method (the reference's ComplexDouble.hpp:283-353 semantics).
+template <class R> __device__ __forceinline__ cx<R> cinv(cx<R> z)
+{
+    if (fabs(z.r) <= fabs(z.i)) {
+        R ratio = z.r / z.i;
+        R rden = R(1) / (z.i * (R(1) + ratio * ratio));
+        return mk(ratio * rden, -rden);
+    } else {
+        R ratio = z.i / z.r;
+        R rden = R(1) / (z.r * (R(1) + ratio * ratio));
+        return mk(rden, -ratio * rden);
+    }
+}
+template <class R> __device__ __forceinline__ cx<R> cdiv(cx<R> a, cx<R> b)
+{
+    if (fabs(b.r) <= fabs(b.i)) {
+        R ratio = b.r / b.i;
+        R rden = R(1) / (b.i * (R(1) + ratio * ratio));
+        return mk((a.r * ratio + a.i) * rden, (a.i * ratio - a.r) * rden);
+    } else {
+        R ratio = b.i / b.r;
+        R rden = R(1) / (b.r * (R(1) + ratio * ratio));
+        return mk((a.r + a.i * ratio) * rden, (a.i - a.r * ratio) * rden);
+    }
+}
+// principal square root (ComplexDouble.hpp:451-488 semantics)
+template <class R> __device__ __forceinline__ cx<R> csqrt(cx<R> z)
+{
+    R zr = sqrt(R(0.5) * (cabs(z) + fabs(z.r)));
+    R zi = (zr == R(0)) ? R(0) : fabs(z.i) / (R(2) * zr);
+    cx<R> w = (z.r < R(0)) ? mk(zi, zr) : mk(zr, zi);
+    if (z.i < R(0)) w.i = -w.i;
+    return w;
+}
+
+template <class R> struct lim;
+template <> struct lim<double> {
+    static __device__ __forceinline__ double eps() { return DBL_EPSILON; }
+    static __device__ __forceinline__ double tiny() { return DBL_MIN; }
+};
+template <> struct lim<float> {
+    static __device__ __forceinline__ float eps() { return FLT_EPSILON; }
+    static __device__ __forceinline__ float tiny() { return FLT_MIN; }
+};
+
+// ---------------------------------------------------------------------------
+// Matrix accessors.  Indices are 1-based (i = row, j = column), column-major.
+// ---------------------------------------------------------------------------
+
+// The reference's structure-of-arrays layout: two planes, element (i,j) of a
+// matrix at ((i-1) + (j-1)*n) * s from the matrix's base (s = thread_cnt).
+template <class R> struct MatSoA {
+    R *re, *im;
+    long long s;
+    int n;
+    __device__ __forceinline__ long long at(int i, int j) const { return ((long long)(i - 1) + (long long)(j - 1) * n) * s; }
+    __device__ __forceinline__ cx<R> ld(int i, int j) const { long long k = at(i, j); return mk(re[k], im[k]); }
+    __device__ __forceinline__ void st(int i, int j, cx<R> v) const { long long k = at(i, j); re[k] = v.r; im[k] = v.i; }
+};
+template <class R> struct VecSoA {
+    R *re, *im;
+    long long s;
+    __device__ __forceinline__ cx<R> ld(int i) const { long long k = (long long)(i - 1) * s; return mk(re[k], im[k]); }
+    __device__ __forceinline__ void st(int i, cx<R> v) const { long long k = (long long)(i - 1) * s; re[k] = v.r; im[k] = v.i; }
+};
+
+template <class R> struct vec2;
+template <> struct vec2<double> { typedef double2 T; };
+template <> struct vec2<float> { typedef float2 T; };
+
+// Workspace layout: (re, im) interleaved, 32 lanes interleaved, so that a warp
+// touching the same element of its 32 matrices issues one contiguous access.
+template <class R> struct MatIlv {
+    typename vec2<R>::T *p;  // already offset by the lane
+    int n;
+    __device__ __forceinline__ cx<R> ld(int i, int j) const
+    {
+        typename vec2<R>::T v = p[((i - 1) + (j - 1) * n) * 32];
+        return mk(v.x, v.y);
+    }
+    __device__ __forceinline__ void st(int i, int j, cx<R> v) const
+    {
+        typename vec2<R>::T w; w.x = v.r; w.y = v.i;
+        p[((i - 1) + (j - 1) * n) * 32] = w;
+    }
+};
+template <class R> struct VecIlv {
+    typename vec2<R>::T *p;
+    __device__ __forceinline__ cx<R> ld(int i) const { typename vec2<R>::T v = p[(i - 1) * 32]; return mk(v.x, v.y); }
+    __device__ __forceinline__ void st(int i, cx<R> v) const { typename vec2<R>::T w; w.x = v.r; w.y = v.i; p[(i - 1) * 32] = w; }
+};
+
+// ---------------------------------------------------------------------------
+// zgehrd: unblocked Householder reduction to upper Hessenberg form
+// (reference Toolbox.hpp:1315-1490, LAPACK zgehd2).  The reflector sign is
+// LAPACK's (beta = -sign(Re alpha) * norm), not the reference's (:1368): the
+// reference's sign makes alpha - beta cancel and divides by zero on columns
+// that are already reduced.  Both give unitarily similar H, so the spectrum
+// and the QR iteration are unaffected.  A column with nothing to annihilate
+// and real alpha gets tau = 0 (LAPACK zlarfg).
+// On exit H holds the Hessenberg matrix on and above the subdiagonal and the
+// reflector vectors below it; tau(i) in `tau`.
+// ---------------------------------------------------------------------------
+template <class R, class M, class V>
+__device__ void zgehrd_lane(const int n, const M &A, const V &tau)
+{
+    for (int i = 1; i <= n - 1; ++i) {
+        const int m = n - i;
+        const cx<R> alpha = A.ld(i + 1, i);
+        R xnorm2 = R(0);
+        for (int k = i + 2; k <= n; ++k) {
+            cx<R> x = A.ld(k, i);
+            xnorm2 += x.r * x.r + x.i * x.i;
+        }
+        const bool trivial = (xnorm2 == R(0)) && (alpha.i == R(0));
+        const R beta = trivial ? alpha.r : -copysign(sqrt(alpha.r * alpha.r + alpha.i * alpha.i + xnorm2), alpha.r);
+        cx<R> t = mk(R(0), R(0));
+        cx<R> scale = mk(R(0), R(0));
+        if (!trivial) {
+            const R rb = R(1) / beta;
+            t = mk((beta - alpha.r) * rb, -alpha.i * rb);
+            scale = cinv(mk(alpha.r - beta, alpha.i));
+        }
+        for (int k = i + 2; k <= n; ++k) A.st(k, i, cmul(A.ld(k, i), scale));
+        tau.st(i, t);
+        // v = [1; A(i+2:n, i)].  Right: A(1:n, i+1:n) -= tau * (A v) v^H, row by row.
+        for (int k = 1; k <= n; ++k) {
+            cx<R> s = A.ld(k, i + 1);
+            for (int j = 2; j <= m; ++j) s = cadd(s, cmul(A.ld(k, i + j), A.ld(i + j, i)));
+            const cx<R> ts = cmul(t, s);
+            A.st(k, i + 1, csub(A.ld(k, i + 1), ts));
+            for (int j = 2; j <= m; ++j) A.st(k, i + j, csub(A.ld(k, i + j), cmulc(ts, A.ld(i + j, i))));
+        }
+        // Left: A(i+1:n, i+1:n) -= conj(tau) * v (v^H A), column by column.
+        const cx<R> tc = conj(t);
+        for (int j = i + 1; j <= n; ++j) {
+            cx<R> s = A.ld(i + 1, j);
+            for (int k = 2; k <= m; ++k) s = cadd(s, cjmul(A.ld(i + k, i), A.ld(i + k, j)));
+            const cx<R> ts = cmul(tc, s);
+            A.st(i + 1, j, csub(A.ld(i + 1, j), ts));
+            for (int k = 2; k <= m; ++k) A.st(i + k, j, csub(A.ld(i + k, j), cmul(A.ld(i + k, i), ts)));
+        }
+        A.st(i + 1, i, mk(beta, R(0)));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// zunghr: form Q = H(1) H(2) ... H(n-1) from the reflectors that zgehrd_lane
+// left below the subdiagonal of A (reference Toolbox.hpp:1492-1659, LAPACK
+// zunghr + zung2r).  The reference first shifts the reflector columns one
+// place right inside Q; here they are read from A directly and Q is written to
+// a separate matrix, which is the same arithmetic.
+// ---------------------------------------------------------------------------
+//
+// Q may be the same storage as A (the reference's in-place call_zunghr): step
+// i reads reflector column i and writes columns i+1..n only, and the first row
+// and column are written last.
+template <class R, class MA, class MQ, class V>
+__device__ void zunghr_lane(const int n, const MA &A, const MQ &Q, const V &tau)
+{
+    // zung2r on Q(2:n, 2:n), reflector i has u(i) = 1, u(i+1:n-1) = A(i+2:n, i)
+    for (int i = n - 1; i >= 1; --i) {
+        const cx<R> t = tau.ld(i);
+        const int c = i + 1;  // global column / row of the reflector's unit entry
+        // apply H(i) from the left to Q(c:n, c+1:n): Q -= tau * u (u^H Q)
+        for (int j = c + 1; j <= n; ++j) {
+            cx<R> s = Q.ld(c, j);
+            for (int k = c + 1; k <= n; ++k) s = cadd(s, cjmul(A.ld(k, i), Q.ld(k, j)));
+            const cx<R> ts = cmul(t, s);
+            Q.st(c, j, csub(Q.ld(c, j), ts));
+            for (int k = c + 1; k <= n; ++k) Q.st(k, j, csub(Q.ld(k, j), cmul(A.ld(k, i), ts)));
+        }
+        // column c: -tau * u below, 1 - tau on the diagonal, zeros above
+        const cx<R> mt = mk(-t.r, -t.i);
+        for (int k = c + 1; k <= n; ++k) Q.st(k, c, cmul(A.ld(k, i), mt));
+        Q.st(c, c, mk(R(1) - t.r, -t.i));
+        for (int k = 2; k <= c - 1; ++k) Q.st(k, c, mk(R(0), R(0)));
+    }
+    // first row and column of Q are those of the identity
+    for (int k = 1; k <= n; ++k) {
+        Q.st(k, 1, mk(R(k == 1), R(0)));
+        if (k > 1) Q.st(1, k, mk(R(0), R(0)));
+    }
+}
+
+// Q = identity (the reference's call_zlahqr_new starts from I, utils.cpp:167-169).
+template <class R, class M>
+__device__ void set_identity_lane(const int n, const M &Q)
+{
+    for (int j = 1; j <= n; ++j)
+        for (int i = 1; i <= n; ++i) Q.st(i, j, mk(R(i == j), R(0)));
+}
+
+// Zero H(i,j) for i >= j+2 (what LAPACK zlahqr does on entry; the reference
+// omits it, Toolbox.hpp:721-723).
+template <class R, class M>
+__device__ void clear_below_subdiag_lane(const int n, const M &H)
+{
+    for (int j = 1; j <= n - 2; ++j)
+        for (int i = j + 2; i <= n; ++i) H.st(i, j, mk(R(0), R(0)));
+}
+
+// ---------------------------------------------------------------------------
+// zlahqr, wantT = wantZ = true: single-shift complex QR with Schur vectors
+// (reference Toolbox.hpp:690-1031 + single_shift_qr_schur :138-369 + scale_rc
+// :14-29; LAPACK zlahqr of the 3.1 generation).  Same deflation criterion
+// (Ahues-Tisseur), exceptional shifts at the 10th and 20th sweep, Wilkinson
+// shift, 2-element reflector bulge chase, and at most max_its+1 sweeps per
+// eigenvalue after which it moves on as the reference does (reported in
+// status).  The deflation test reads Re H(K+1,K) where the reference reads
+// its imaginary part (:840); subdiagonals are real here, so the reference
+// term is always zero -- the difference only shows when two adjacent diagonal
+// entries are exactly zero.
+//
+// Warp-cooperative: must be called by all 32 lanes; `valid` marks lanes that
+// own a matrix.  Every lane keeps its own (I, L, its); a sweep round runs the
+// K loop over the union of the lanes' windows with a warp-uniform K, so each
+// matrix element access is the same offset for all lanes.
+// ---------------------------------------------------------------------------
+template <class R, class MH, class MZ>
+__device__ void make_subdiag_real_lane(const int n, const MH &H, const MZ &Z)
+{
+    for (int i = 2; i <= n; ++i) {
+        const cx<R> h = H.ld(i, i - 1);
+        if (h.i != R(0)) {
+            cx<R> sc = cscal(h, R(1) / cabs1(h));
+            sc = cscal(conj(sc), R(1) / cabs(sc));
+            H.st(i, i - 1, mk(cabs(h), R(0)));
+            for (int j = i; j <= n; ++j) H.st(i, j, cmul(H.ld(i, j), sc));
+            const int re = (i + 1) < n ? (i + 1) : n;
+            for (int j = 1; j <= re; ++j) H.st(j, i, cmulc(H.ld(j, i), sc));
+            for (int j = 1; j <= n; ++j) Z.st(j, i, cmulc(Z.ld(j, i), sc));
+        }
+    }
+}
+
+// Scan for a negligible subdiagonal in rows I..L+1 (reference :810-867).
+template <class R, class MH>
+__device__ __forceinline__ int deflation_scan(const int I, const int L0, const MH &H, const int n, const R ulp, const R smlnum)
+{
+    int K;
+    for (K = I; K >= L0 + 1; --K) {
+        const cx<R> hk = H.ld(K, K - 1);
+        if (cabs1(hk) <= smlnum) break;
+        const cx<R> hkm = H.ld(K - 1, K - 1), hkk = H.ld(K, K);
+        R tst = cabs1(hkm) + cabs1(hkk);
+        if (tst == R(0)) {
+            if (K - 2 >= 1) tst += fabs(H.ld(K - 1, K - 2).r);
+            if (K + 1 <= n) tst += fabs(H.ld(K + 1, K).r);
+        }
+        if (fabs(hk.r) <= ulp * tst) {
+            R d2 = cabs1(hk), d3 = cabs1(H.ld(K - 1, K));
+            const R ab = fmax(d2, d3), ba = fmin(d2, d3);
+            d2 = cabs1(hkk);
+            d3 = cabs1(csub(hkm, hkk));
+            const R aa = fmax(d2, d3), bb = fmin(d2, d3);
+            const R s = aa + ab;
+            if (ba * (ab / s) <= fmax(smlnum, ulp * (bb * (aa / s)))) break;
+        }
+    }
+    return K;
+}
+
+// Shift for sweep number `its` on the active block L..I (reference :896-990).
+template <class R, class MH>
+__device__ __forceinline__ cx<R> qr_shift(const int I, const int L, const int its, const MH &H)
+{
+    if (its == 10) return cadd(mk(R(0.75) * fabs(H.ld(L + 1, L).r), R(0)), H.ld(L, L));
+    if (its == 20) return cadd(mk(R(0.75) * fabs(H.ld(I, I - 1).r), R(0)), H.ld(I, I));
+    cx<R> t = H.ld(I, I);
+    const cx<R> u = cmul(csqrt(H.ld(I - 1, I)), csqrt(H.ld(I, I - 1)));
+    R s = cabs1(u);
+    if (s != R(0)) {
+        const cx<R> x = cscal(csub(H.ld(I - 1, I - 1), t), R(0.5));
+        const R sx = cabs1(x);
+        s = fmax(s, sx);
+        const R rs = R(1) / s;
+        const cx<R> xs = cscal(x, rs), us = cscal(u, rs);
+        cx<R> y = cscal(csqrt(cadd(cmul(xs, xs), cmul(us, us))), s);
+        if (sx > R(0)) {
+            const R rsx = R(1) / sx;
+            if ((x.r * rsx) * y.r + (x.i * rsx) * y.i < R(0)) y = mk(-y.r, -y.i);
+        }
+        t = csub(t, cmul(cdiv(u, cadd(x, y)), u));
+    }
+    return t;
+}
+
+// 2-element Householder reflector for (v0, v1) (reference :186-241, LAPACK
+// zlarfg with n = 2).  Returns tau in t1, overwrites v1 with the scaled vector
+// entry and v0 with the new leading entry.
+template <class R>
+__device__ __forceinline__ void zlarfg2(cx<R> &v0, cx<R> &v1, cx<R> &t1)
+{
+    if (v1.r == R(0) && v1.i == R(0) && v0.i == R(0)) {
+        t1 = mk(R(0), R(0));
+        return;
+    }
+    const R safmin = lim<R>::tiny() / (lim<R>::eps() * R(0.5));
+    R norm = sqrt(v0.r * v0.r + v0.i * v0.i + v1.r * v1.r + v1.i * v1.i);
+    int knt = 0;
+    if (norm < safmin) {
+        const R rs = R(1) / safmin;
+        do {
+            ++knt;
+            v1 = cscal(v1, rs);
+            v0 = cscal(v0, rs);
+            norm *= rs;
+        } while (norm < safmin && knt < 40);
+        norm = sqrt(v0.r * v0.r + v0.i * v0.i + v1.r * v1.r + v1.i * v1.i);
+    }
+    R beta = copysign(norm, v0.r);
+    const cx<R> z = mk(v0.r + beta, v0.i);
+    t1 = cscal(z, R(1) / beta);
+    v1 = cmul(v1, cinv(z));
+    for (int q = 0; q < knt; ++q) beta *= safmin;
+    v0 = mk(-beta, R(0));
+}
+
+template <class R, class MH, class MZ>
+__device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool valid, const int max_its,
+                            int &nsweeps, int &status)
+{
+    const R ulp = lim<R>::eps();
+    const R smlnum = lim<R>::tiny() * (R(n) / ulp);
+    if (valid) make_subdiag_real_lane<R>(n, H, Z);
+
+    // Lane state: active block L..I and the sweep count at this I.  As in the
+    // reference, L only moves up while I stays, and resets to 1 when I moves.
+    int I = n, L = 1, its = 0;
+    bool done = !valid || n <= 1;
+    for (;;) {
+        bool sweep = false;
+        cx<R> v0 = mk(R(0), R(0)), v1 = mk(R(0), R(0));
+        if (!done) {
+            for (;;) {
+                if (I <= 1) { done = true; break; }
+                if (its > max_its) { status |= ST_ITCAP; --I; L = 1; its = 0; continue; }
+                L = deflation_scan<R>(I, L, H, n, ulp, smlnum);
+                if (L > 1) H.st(L, L - 1, mk(R(0), R(0)));
+                if (L >= I) { --I; L = 1; its = 0; continue; }
+                const cx<R> t = qr_shift<R>(I, L, its, H);
+                const cx<R> h11s = csub(H.ld(L, L), t);
+                const R h21 = H.ld(L + 1, L).r;
+                const R rs = R(1) / (cabs1(h11s) + fabs(h21));
+                v0 = cscal(h11s, rs);
+                v1 = mk(h21 * rs, R(0));
+                sweep = true;
+                ++its;
+                ++nsweeps;
+                break;
+            }
+        }
+        if (!__any_sync(FULL, sweep)) break;  // every lane is done
+        const int Kmin = __reduce_min_sync(FULL, sweep ? L : INT_MAX);
+        const int Kmax = __reduce_max_sync(FULL, sweep ? I - 1 : 0);
+        for (int K = Kmin; K <= Kmax; ++K) {
+            const bool act = sweep && K >= L && K <= I - 1;
+            cx<R> t1 = mk(R(0), R(0)), w1 = mk(R(0), R(0));
+            if (act) {
+                cx<R> a0 = v0, a1 = v1;
+                if (K > L) { a0 = H.ld(K, K - 1); a1 = H.ld(K + 1, K - 1); }
+                zlarfg2<R>(a0, a1, t1);
+                if (K > L) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(R(0), R(0))); }
+                w1 = a1;
+            }
+            const R t2 = t1.r * w1.r - t1.i * w1.i;
+            if (act) {
+                // rows K, K+1, columns K..n (wantT: I2 = n)
+                for (int j = K; j <= n; ++j) {
+                    const cx<R> h1 = H.ld(K, j), h2 = H.ld(K + 1, j);
+                    const cx<R> z = cadd(cmulc(h1, t1), cscal(h2, t2));
+                    H.st(K, j, csub(h1, z));
+                    H.st(K + 1, j, csub(h2, cmul(z, w1)));
+                }
+            }
+            // columns K, K+1, rows 1..min(K+2, I)
+            const int je = (K + 2) < n ? (K + 2) : n;
+            for (int j = 1; j <= je; ++j) {
+                if (act && j <= I) {
+                    const cx<R> h1 = H.ld(j, K), h2 = H.ld(j, K + 1);
+                    const cx<R> z = cadd(cmul(h1, t1), cscal(h2, t2));
+                    H.st(j, K, csub(h1, z));
+                    H.st(j, K + 1, csub(h2, cmulc(z, w1)));
+                }
+            }
+            if (act) {
+                for (int j = 1; j <= n; ++j) {
+                    const cx<R> z1 = Z.ld(j, K), z2 = Z.ld(j, K + 1);
+                    const cx<R> z = cadd(cmul(z1, t1), cscal(z2, t2));
+                    Z.st(j, K, csub(z1, z));
+                    Z.st(j, K + 1, csub(z2, cmulc(z, w1)));
+                }
+            }
+        }
+        if (sweep) {
+            // make H(I, I-1) real (reference :337-367)
+            const cx<R> h = H.ld(I, I - 1);
+            if (h.i != R(0)) {
+                const R d = cabs(h);
+                const cx<R> z = conj(cscal(h, R(1) / d));
+                H.st(I, I - 1, mk(d, R(0)));
+                for (int j = I + 1; j <= n; ++j) H.st(I, j, cmul(H.ld(I, j), z));
+                for (int j = 1; j <= I - 1; ++j) H.st(j, I, cmulc(H.ld(j, I), z));
+                for (int j = 1; j <= n; ++j) Z.st(j, I, cmulc(Z.ld(j, I), z));
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// ztrevc: right eigenvectors of the upper-triangular T, back-transformed by
+// the Schur vectors R in place (reference Toolbox.hpp:1133-1313 with the
+// back substitution of :31-136; LAPACK ztrevc SIDE='R', HOWMNY='B').  The
+// shifted diagonal T(k,k) - T(ki,ki), clamped to smin as in the reference, is
+// formed on the fly, so T is read only.  x is held in the work vector `x`.
+// Eigenvector ki comes out as R * [x; 1; 0], the reference's scaling.
+// ---------------------------------------------------------------------------
+template <class R, class MT, class MR, class V>
+__device__ void ztrevc_lane(const int n, const MT &T, const MR &Rm, const V &x)
+{
+    const R ulp = lim<R>::eps();
+    const R smlnum = lim<R>::tiny() * (R(n) / ulp);
+    for (int ki = n; ki >= 2; --ki) {
+        const cx<R> tkk = T.ld(ki, ki);
+        const R smin = fmax(ulp * cabs1(tkk), smlnum);
+        for (int k = 1; k <= ki - 1; ++k) { const cx<R> v = T.ld(k, ki); x.st(k, mk(-v.r, -v.i)); }
+        // back substitution with (T(1:ki-1,1:ki-1) - T(ki,ki) I)
+        for (int j = ki - 1; j >= 1; --j) {
+            cx<R> d = csub(T.ld(j, j), tkk);
+            if (cabs1(d) < smin) d = mk(smin, R(0));
+            const cx<R> xj = cdiv(x.ld(j), d);
+            x.st(j, xj);
+            for (int i = j - 1; i >= 1; --i) x.st(i, csub(x.ld(i), cmul(T.ld(i, j), xj)));
+        }
+        // R(:, ki) := R(:, 1:ki-1) x + R(:, ki)
+        for (int i = 1; i <= n; ++i) {
+            cx<R> acc = Rm.ld(i, ki);
+            for (int j = 1; j <= ki - 1; ++j) acc = cadd(acc, cmul(Rm.ld(i, j), x.ld(j)));
+            Rm.st(i, ki, acc);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Small BLAS-2 helpers of the reference's test surface.
+// ---------------------------------------------------------------------------
+
+// y := A x + beta y, or A^H x + beta y (reference zgemv_simple Toolbox.hpp:1033-1131
+// on the full matrix; its Hermitian branch reads Re(y) for Im(y) (:1125) -- here
+// the imaginary part is read).
+template <class R, class M, class V>
+__device__ void zgemv_lane(const bool herm, const int n, const M &A, const V &x, const cx<R> beta, const V &y)
+{
+    for (int i = 1; i <= n; ++i) y.st(i, cmul(y.ld(i), beta));
+    if (!herm) {
+        for (int j = 1; j <= n; ++j) {
+            const cx<R> xj = x.ld(j);
+            for (int i = 1; i <= n; ++i) y.st(i, cadd(y.ld(i), cmul(A.ld(i, j), xj)));
+        }
+    } else {
+        for (int j = 1; j <= n; ++j) {
+            cx<R> acc = mk(R(0), R(0));
+            for (int i = 1; i <= n; ++i) acc = cadd(acc, cmulc(x.ld(i), A.ld(i, j)));
+            y.st(j, cadd(y.ld(j), acc));
+        }
+    }
+}
+
+// Solve T x = b for upper-triangular T, b in x (reference Toolbox.hpp:31-136).
+template <class R, class M, class V>
+__device__ void backsubs_lane(const int n, const M &T, const V &x)
+{
+    for (int j = n; j >= 1; --j) {
+        const cx<R> xj = cdiv(x.ld(j), T.ld(j, j));
+        x.st(j, xj);
+        for (int i = j - 1; i >= 1; --i) x.st(i, csub(x.ld(i), cmul(T.ld(i, j), xj)));
+    }
+}
+
+// Bit test for Inf/NaN without touching the FP64 pipe.
+__device__ __forceinline__ bool nonfinite(double v)
+{
+    return (__double2hiint(v) & 0x7ff00000) == 0x7ff00000;
+}
+__device__ __forceinline__ bool nonfinite(float v)
+{
+    return (__float_as_uint(v) & 0x7f800000u) == 0x7f800000u;
+}
+
+}  // namespace ves

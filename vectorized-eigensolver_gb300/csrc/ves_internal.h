@@ -1,0 +1,48 @@
+// ves_internal.h -- launchers shared by the C-ABI layer (ves_api.cu) and the
+// kernels (ves_kernels.cu).  Not part of the public interface.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+
+namespace ves {
+
+// Batch geometry of the reference's SoA layout: N = block_cnt * thread_cnt
+// matrices of order n, interleave stride tc = thread_cnt.
+struct Geom {
+    int n;
+    long long N;
+    int tc;
+};
+
+struct FusedArgs {
+    Geom g;
+    const double *rA, *iA;  // input (read only)
+    double *rE, *iE;        // eigenvalues, SoA vector layout
+    double *rV, *iV;        // eigenvectors, SoA matrix layout
+    double *rT, *iT;        // optional Schur form T (may alias rA/iA)
+    int *status;            // optional, one per matrix (plain index order)
+    int *sweeps;            // optional, QR sweeps per matrix
+    void *ws;               // workspace
+    int max_its;
+    int vnorm;
+};
+
+// Fused zgehrd -> zunghr -> zlahqr -> ztrevc, FP64.
+size_t fused_workspace_bytes(int n, long long N, int *out_blocks, int *out_threads);
+cudaError_t launch_fused_fp64(const FusedArgs &a, cudaStream_t st);
+
+// Stage kernels, in place on the SoA layout (reference call_* semantics).
+cudaError_t launch_zgehrd(Geom g, double *rA, double *iA, double *rtau, double *itau, cudaStream_t st);
+cudaError_t launch_zunghr(Geom g, double *rA, double *iA, const double *rtau, const double *itau, cudaStream_t st);
+cudaError_t launch_hessenberg(Geom g, double *rA, double *iA, double *rQ, double *iQ, double *rtau, double *itau,
+                              cudaStream_t st);
+cudaError_t launch_zlahqr(Geom g, double *rE, double *iE, double *rH, double *iH, double *rZ, double *iZ,
+                          int *status, int max_its, cudaStream_t st);
+cudaError_t launch_ztrevc(Geom g, double *rT, double *iT, double *rR, double *iR, double *rwork, double *iwork,
+                          cudaStream_t st);
+cudaError_t launch_zgemv(Geom g, bool herm, const double *rA, const double *iA, const double *rx, const double *ix,
+                         double rbeta, double ibeta, double *ry, double *iy, cudaStream_t st);
+cudaError_t launch_backsubs(Geom g, const double *rT, const double *iT, double *rx, double *ix, cudaStream_t st);
+
+}  // namespace ves

@@ -1,0 +1,305 @@
+// ves_kernels.cu -- sm_103a kernels of the batched eigensolver.
+//
+// fused_fp64_kernel: the whole path of the reference's eigensolver()
+// (utils.cpp:578-698: test_zgehrd -> copy -> test_zunghr -> zlahqr_new ->
+// test_ztrevc, Toolbox.hpp:2150/2179/1984/2060) in one launch.  Each warp is
+// persistent and takes groups of 32 consecutive matrices; lane l of a group
+// owns matrix 32*g + l.  The input is read once from the SoA layout, the
+// working H and Z live in a per-warp workspace laid out so that the 32 lanes'
+// copies of one element are contiguous (one 512-byte access per warp), and
+// eigenvalues / eigenvectors are written once.
+//
+// The stage kernels implement the reference's per-stage entry points
+// (call_zgehrd, call_zunghr, hessenberg, call_zlahqr_new, call_ztrevc,
+// call_zgemv, call_backsubstitution) in place on the SoA layout, one matrix
+// per lane.
+#include "ves_device.cuh"
+#include "ves_internal.h"
+
+#include <algorithm>
+#include <cstdlib>
+
+namespace ves {
+
+namespace {
+
+constexpr int kFusedThreads = 128;  // 4 warps per block
+
+__device__ __forceinline__ long long soa_mat_off(long long m, int n, int tc)
+{
+    return (m / tc) * (long long)tc * n * n + (m % tc);
+}
+__device__ __forceinline__ long long soa_vec_off(long long m, int n, int tc)
+{
+    return (m / tc) * (long long)tc * n + (m % tc);
+}
+
+// Eigenvector column scaling: 0 = as the reference leaves it (the T-eigenvector
+// has a unit entry at position k), 1 = largest |re|+|im| equal to 1 (LAPACK
+// ztrevc), 2 = unit 2-norm.
+template <class R, class MZ>
+__device__ void write_vectors(const int n, const MZ &Z, const MatSoA<R> &V, const int vnorm)
+{
+    for (int j = 1; j <= n; ++j) {
+        R scale = R(1);
+        if (vnorm == 1) {
+            R mx = R(0);
+            for (int i = 1; i <= n; ++i) mx = fmax(mx, cabs1(Z.ld(i, j)));
+            scale = mx > R(0) ? R(1) / mx : R(1);
+        } else if (vnorm == 2) {
+            R s2 = R(0);
+            for (int i = 1; i <= n; ++i) { const cx<R> z = Z.ld(i, j); s2 += z.r * z.r + z.i * z.i; }
+            scale = s2 > R(0) ? R(1) / sqrt(s2) : R(1);
+        }
+        for (int i = 1; i <= n; ++i) V.st(i, j, cscal(Z.ld(i, j), scale));
+    }
+}
+
+__global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedArgs a)
+{
+    const int n = a.g.n, tc = a.g.tc;
+    const long long N = a.g.N;
+    const int lane = threadIdx.x & 31;
+    const long long slot = (long long)blockIdx.x * (kFusedThreads / 32) + (threadIdx.x >> 5);
+    const long long nslots = (long long)gridDim.x * (kFusedThreads / 32);
+    const long long ngroups = (N + 31) / 32;
+    const long long per_lane = 2LL * n * n + n;  // H, Z, work vector
+
+    double2 *base = reinterpret_cast<double2 *>(a.ws) + slot * per_lane * 32 + lane;
+    const MatIlv<double> H{base, n};
+    const MatIlv<double> Z{base + (long long)n * n * 32, n};
+    const VecIlv<double> W{base + 2LL * n * n * 32};
+
+    for (long long g = slot; g < ngroups; g += nslots) {
+        const long long m = g * 32 + lane;
+        const bool valid = m < N;
+        const long long mo = valid ? soa_mat_off(m, n, tc) : 0;
+        const long long vo = valid ? soa_vec_off(m, n, tc) : 0;
+        int status = 0, sweeps = 0;
+
+        if (valid) {
+            const MatSoA<double> A{const_cast<double *>(a.rA) + mo, const_cast<double *>(a.iA) + mo, tc, n};
+            bool bad = false;
+            for (int j = 1; j <= n; ++j)
+                for (int i = 1; i <= n; ++i) {
+                    const cx<double> v = A.ld(i, j);
+                    bad |= nonfinite(v.r) | nonfinite(v.i);
+                    H.st(i, j, v);
+                }
+            if (bad) status |= ST_NONFINITE;
+            zgehrd_lane<double>(n, H, W);
+            zunghr_lane<double>(n, H, Z, W);
+            clear_below_subdiag_lane<double>(n, H);
+        }
+        zlahqr_warp<double>(n, H, Z, valid && !(status & ST_NONFINITE), a.max_its, sweeps, status);
+        if (valid) {
+            const VecSoA<double> E{a.rE + vo, a.iE + vo, tc};
+            for (int k = 1; k <= n; ++k) E.st(k, H.ld(k, k));
+            if (a.rT) {
+                const MatSoA<double> T{a.rT + mo, a.iT + mo, tc, n};
+                for (int j = 1; j <= n; ++j)
+                    for (int i = 1; i <= n; ++i) T.st(i, j, i <= j ? H.ld(i, j) : mk(0.0, 0.0));
+            }
+            ztrevc_lane<double>(n, H, Z, W);
+            const MatSoA<double> V{a.rV + mo, a.iV + mo, tc, n};
+            write_vectors<double>(n, Z, V, a.vnorm);
+            if (a.status) a.status[m] = status;
+            if (a.sweeps) a.sweeps[m] = sweeps;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Stage kernels: one lane per matrix, in place on the SoA layout.
+// ---------------------------------------------------------------------------
+struct Lane {
+    long long m;
+    bool valid;
+    long long mo, vo;
+};
+__device__ __forceinline__ Lane lane_of(const Geom &g)
+{
+    Lane l;
+    l.m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    l.valid = l.m < g.N;
+    l.mo = l.valid ? soa_mat_off(l.m, g.n, g.tc) : 0;
+    l.vo = l.valid ? soa_vec_off(l.m, g.n, g.tc) : 0;
+    return l;
+}
+
+__global__ void zgehrd_kernel(const Geom g, double *rA, double *iA, double *rtau, double *itau)
+{
+    const Lane l = lane_of(g);
+    if (!l.valid) return;
+    const MatSoA<double> A{rA + l.mo, iA + l.mo, g.tc, g.n};
+    const VecSoA<double> tau{rtau + l.vo, itau + l.vo, g.tc};
+    zgehrd_lane<double>(g.n, A, tau);
+}
+
+__global__ void zunghr_kernel(const Geom g, double *rA, double *iA, const double *rtau, const double *itau)
+{
+    const Lane l = lane_of(g);
+    if (!l.valid) return;
+    const MatSoA<double> A{rA + l.mo, iA + l.mo, g.tc, g.n};
+    const VecSoA<double> tau{const_cast<double *>(rtau) + l.vo, const_cast<double *>(itau) + l.vo, g.tc};
+    zunghr_lane<double>(g.n, A, A, tau);
+}
+
+// hessenberg(): A -> H (reflectors below the subdiagonal, as the reference
+// leaves them), Q formed in a separate matrix.
+__global__ void hessenberg_kernel(const Geom g, double *rA, double *iA, double *rQ, double *iQ, double *rtau,
+                                  double *itau)
+{
+    const Lane l = lane_of(g);
+    if (!l.valid) return;
+    const MatSoA<double> A{rA + l.mo, iA + l.mo, g.tc, g.n};
+    const MatSoA<double> Q{rQ + l.mo, iQ + l.mo, g.tc, g.n};
+    const VecSoA<double> tau{rtau + l.vo, itau + l.vo, g.tc};
+    zgehrd_lane<double>(g.n, A, tau);
+    zunghr_lane<double>(g.n, A, Q, tau);
+}
+
+// call_zlahqr_new(): Z := I, H (cleared below the subdiagonal) -> T, E = diag(T).
+__global__ void zlahqr_kernel(const Geom g, double *rE, double *iE, double *rH, double *iH, double *rZ, double *iZ,
+                              int *status_out, int max_its)
+{
+    const Lane l = lane_of(g);
+    const MatSoA<double> H{rH + l.mo, iH + l.mo, g.tc, g.n};
+    const MatSoA<double> Z{rZ + l.mo, iZ + l.mo, g.tc, g.n};
+    int status = 0, sweeps = 0;
+    if (l.valid) {
+        set_identity_lane<double>(g.n, Z);
+        clear_below_subdiag_lane<double>(g.n, H);
+    }
+    zlahqr_warp<double>(g.n, H, Z, l.valid, max_its, sweeps, status);
+    if (l.valid) {
+        const VecSoA<double> E{rE + l.vo, iE + l.vo, g.tc};
+        for (int k = 1; k <= g.n; ++k) E.st(k, H.ld(k, k));
+        if (status_out) status_out[l.m] = status;
+    }
+}
+
+__global__ void ztrevc_kernel(const Geom g, double *rT, double *iT, double *rR, double *iR, double *rw, double *iw)
+{
+    const Lane l = lane_of(g);
+    if (!l.valid) return;
+    const MatSoA<double> T{rT + l.mo, iT + l.mo, g.tc, g.n};
+    const MatSoA<double> Rm{rR + l.mo, iR + l.mo, g.tc, g.n};
+    const VecSoA<double> x{rw + l.vo, iw + l.vo, g.tc};
+    ztrevc_lane<double>(g.n, T, Rm, x);
+}
+
+__global__ void zgemv_kernel(const Geom g, bool herm, const double *rA, const double *iA, const double *rx,
+                             const double *ix, double rbeta, double ibeta, double *ry, double *iy)
+{
+    const Lane l = lane_of(g);
+    if (!l.valid) return;
+    const MatSoA<double> A{const_cast<double *>(rA) + l.mo, const_cast<double *>(iA) + l.mo, g.tc, g.n};
+    const VecSoA<double> x{const_cast<double *>(rx) + l.vo, const_cast<double *>(ix) + l.vo, g.tc};
+    const VecSoA<double> y{ry + l.vo, iy + l.vo, g.tc};
+    zgemv_lane<double>(herm, g.n, A, x, mk(rbeta, ibeta), y);
+}
+
+__global__ void backsubs_kernel(const Geom g, const double *rT, const double *iT, double *rx, double *ix)
+{
+    const Lane l = lane_of(g);
+    if (!l.valid) return;
+    const MatSoA<double> T{const_cast<double *>(rT) + l.mo, const_cast<double *>(iT) + l.mo, g.tc, g.n};
+    const VecSoA<double> x{rx + l.vo, ix + l.vo, g.tc};
+    backsubs_lane<double>(g.n, T, x);
+}
+
+constexpr int kStageThreads = 128;
+inline unsigned stage_blocks(const Geom &g) { return (unsigned)((g.N + kStageThreads - 1) / kStageThreads); }
+
+int g_fused_blocks_per_sm = 2;  // 8 warps per SM; tunable through VES_FUSED_BLOCKS_PER_SM
+
+}  // namespace
+
+size_t fused_workspace_bytes(int n, long long N, int *out_blocks, int *out_threads)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+    static bool env_read = false;
+    if (!env_read) {
+        env_read = true;
+        if (const char *e = getenv("VES_FUSED_BLOCKS_PER_SM")) {
+            int v = atoi(e);
+            if (v >= 1 && v <= 16) g_fused_blocks_per_sm = v;
+        }
+    }
+    const long long groups = (N + 31) / 32;
+    const int wpb = kFusedThreads / 32;
+    long long blocks = std::min<long long>((groups + wpb - 1) / wpb, (long long)sms * g_fused_blocks_per_sm);
+    if (blocks < 1) blocks = 1;
+    const size_t per_slot = (size_t)(2LL * n * n + n) * 32 * sizeof(double2);
+    if (out_blocks) *out_blocks = (int)blocks;
+    if (out_threads) *out_threads = kFusedThreads;
+    return per_slot * (size_t)blocks * wpb;
+}
+
+cudaError_t launch_fused_fp64(const FusedArgs &a, cudaStream_t st)
+{
+    if (a.g.N <= 0) return cudaSuccess;
+    int blocks = 0, threads = 0;
+    fused_workspace_bytes(a.g.n, a.g.N, &blocks, &threads);
+    fused_fp64_kernel<<<blocks, threads, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zgehrd(Geom g, double *rA, double *iA, double *rtau, double *itau, cudaStream_t st)
+{
+    if (g.N <= 0) return cudaSuccess;
+    zgehrd_kernel<<<stage_blocks(g), kStageThreads, 0, st>>>(g, rA, iA, rtau, itau);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zunghr(Geom g, double *rA, double *iA, const double *rtau, const double *itau, cudaStream_t st)
+{
+    if (g.N <= 0) return cudaSuccess;
+    zunghr_kernel<<<stage_blocks(g), kStageThreads, 0, st>>>(g, rA, iA, rtau, itau);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hessenberg(Geom g, double *rA, double *iA, double *rQ, double *iQ, double *rtau, double *itau,
+                              cudaStream_t st)
+{
+    if (g.N <= 0) return cudaSuccess;
+    hessenberg_kernel<<<stage_blocks(g), kStageThreads, 0, st>>>(g, rA, iA, rQ, iQ, rtau, itau);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zlahqr(Geom g, double *rE, double *iE, double *rH, double *iH, double *rZ, double *iZ,
+                          int *status, int max_its, cudaStream_t st)
+{
+    if (g.N <= 0) return cudaSuccess;
+    zlahqr_kernel<<<stage_blocks(g), kStageThreads, 0, st>>>(g, rE, iE, rH, iH, rZ, iZ, status, max_its);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ztrevc(Geom g, double *rT, double *iT, double *rR, double *iR, double *rw, double *iw,
+                          cudaStream_t st)
+{
+    if (g.N <= 0) return cudaSuccess;
+    ztrevc_kernel<<<stage_blocks(g), kStageThreads, 0, st>>>(g, rT, iT, rR, iR, rw, iw);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zgemv(Geom g, bool herm, const double *rA, const double *iA, const double *rx, const double *ix,
+                         double rbeta, double ibeta, double *ry, double *iy, cudaStream_t st)
+{
+    if (g.N <= 0) return cudaSuccess;
+    zgemv_kernel<<<stage_blocks(g), kStageThreads, 0, st>>>(g, herm, rA, iA, rx, ix, rbeta, ibeta, ry, iy);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_backsubs(Geom g, const double *rT, const double *iT, double *rx, double *ix, cudaStream_t st)
+{
+    if (g.N <= 0) return cudaSuccess;
+    backsubs_kernel<<<stage_blocks(g), kStageThreads, 0, st>>>(g, rT, iT, rx, ix);
+    return cudaGetLastError();
+}
+
+}  // namespace ves
