@@ -1,0 +1,401 @@
+"""Benchmark: batched complex eigen-decomposition on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ves|reference]
+
+Workload (one step = one solve of the whole batch): 1,048,576 complex128
+16x16 matrices, real and imaginary parts i.i.d. N(0,1) from numpy
+default_rng(1), in the reference's SoA layout with thread_cnt = 512; all
+eigenvalues and right eigenvectors (zgehrd -> zunghr -> zlahqr -> ztrevc).
+The input (4.3 GB) is larger than L2, so no flush is needed between steps.
+
+value   eigensolves/s with the batch resident in HBM, CUDA events around K
+        launches of ves_eigensolve on the launching stream.
+e2e     the same metric through the reference-facing drop-in eigensolver()
+        with pinned HOST buffers: host->device copy of A, solve, device->host
+        copy of eigenvalues, eigenvectors and the Schur form (which the
+        reference API writes back into A) inside the timed region.
+roofline  the solver is FP64-pipe bound: achieved = algorithmic FP64 flops
+        per launch (24 n^3 + 20 s n^3 per matrix, s = device-counted QR
+        sweeps per eigenvalue) / launch time, against the FP64 FMA rate
+        measured on this GPU in this run (MEASURED_PEAKS.json carries no FP64
+        figure).  The HBM view (32 n^2 + 16 n bytes per matrix) is reported
+        beside it.
+cpu_baseline  the oracle's C restatement of the reference CPU path (OpenMP,
+        all host cores) on a bounded prefix of the same batch.
+Every result is verified after timing: all residuals on the device in FP64
+(<= 1e-13 of ||A||_F ||v||); eigenvalue parity with the oracle is the job of
+the test suite (tests/test_gpu_fullsize.py runs this workload).
+
+--impl reference times the reference's CPU implementation of the path on the
+host cores (the compiled reference where it was built, otherwise the C
+restatement) on bounded samples of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "vectorized-eigensolver_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "eigensolves/s at n=16,32 at resid≤1e-13; learned-shift, FP32+refine vs plain FP64"
+WORKLOAD = dict(name="gauss16", N=1_048_576, n=16, seed=1, tc=512)
+RES_TOL = 1e-13
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ----------------------------------------------------------------------------
+# distributed plumbing (one process per GPU; independent replicas, no data-path collective)
+# ----------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+
+    def init(self, backend):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64, device="cuda" if self.pg.get_backend() == "nccl" else "cpu")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def done(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------
+# clocks during the timed region
+# ----------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------
+# CPU side: the oracle (test infrastructure, used here only as the timed baseline)
+# ----------------------------------------------------------------------------
+def cpu_time(rA, iA, n, tc, threads, lib, min_seconds):
+    import oracle
+    N = rA.size // (n * n)
+    reps, total = 0, 0.0
+    oracle.eigensolve(rA, iA, n, tc, lib=lib, threads=threads)  # warm-up
+    while total < min_seconds:
+        t0 = time.perf_counter()
+        oracle.eigensolve(rA, iA, n, tc, lib=lib, threads=threads)
+        total += time.perf_counter() - t0
+        reps += 1
+    return N * reps / total, reps, total
+
+
+def cpu_kind():
+    import oracle
+    return ("reference", "reference") if oracle.reference() is not None else ("port", "restatement")
+
+
+# ----------------------------------------------------------------------------
+def run_reference_arm(args, d):
+    if d.rank != 0:
+        return
+    w = WORKLOAD
+    import workloads
+    cores = os.cpu_count() or 1
+    kind, lib = cpu_kind()
+    sample = 65_536
+    rA, iA = workloads.gaussian_soa(w["N"], w["n"], w["seed"], w["tc"])
+    k = sample * w["n"] ** 2
+    rA, iA = rA[:k].copy(), iA[:k].copy()
+    for _ in range(max(args.warmup, 0)):
+        cpu_time(rA, iA, w["n"], w["tc"], cores, lib, 0.0)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        import oracle
+        oracle.eigensolve(rA, iA, w["n"], w["tc"], lib=lib, threads=cores)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    val = sample * args.steps / tot
+    out = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "eigensolves/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: complex Gaussian, numpy default_rng(1)",
+        "config": {"workload": "1,048,576 complex128 16x16 (SoA thread_cnt=512, seed 1); each step solves "
+                               "its first %d matrices on the host CPU" % sample, "n": w["n"]},
+        "cpu_baseline": {"value": val, "unit": "eigensolves/s", "cores": cores, "kind": kind,
+                         "sample": "first %d matrices of the batch per step, zgehrd->zunghr->zlahqr->ztrevc, "
+                                   "OpenMP over all %d host threads" % (sample, cores)},
+        "e2e": {"value": val, "unit": "eigensolves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def device_residual_check(dAr, dAi, dEr, dEi, dVr, dVi, n, tc, chunk=1 << 17):
+    """max over all pairs of ||A v - lambda v|| / (||A||_F ||v||), FP64 on the device."""
+    import torch
+
+    def mat(re, im):
+        return torch.complex(re.view(-1, n, n, tc).permute(0, 3, 2, 1), im.view(-1, n, n, tc).permute(0, 3, 2, 1)
+                             ).reshape(-1, n, n)
+    A, V = mat(dAr, dAi), mat(dVr, dVi)
+    E = torch.complex(dEr.view(-1, n, tc).permute(0, 2, 1), dEi.view(-1, n, tc).permute(0, 2, 1)).reshape(-1, n)
+    worst, nonfinite = 0.0, 0
+    for s in range(0, A.shape[0], chunk):
+        a, e, v = A[s:s + chunk], E[s:s + chunk], V[s:s + chunk]
+        r = torch.linalg.vector_norm(torch.matmul(a, v) - v * e[:, None, :], dim=1)
+        den = torch.linalg.matrix_norm(a)[:, None] * torch.linalg.vector_norm(v, dim=1)
+        q = r / den
+        nonfinite += int((~torch.isfinite(q)).sum())
+        worst = max(worst, float(torch.nan_to_num(q, nan=0.0).max()))
+    return {"max_residual": worst, "nonfinite": nonfinite, "checked_matrices": int(A.shape[0])}
+
+
+def flops_per_matrix(n, s):
+    return 24.0 * n ** 3 + 20.0 * s * n ** 3
+
+
+def run_gpu_arm(args, d):
+    import torch
+    import ves
+    import workloads
+
+    torch.cuda.set_device(d.local)
+    d.init("nccl")
+    w = WORKLOAD
+    N, n, tc = w["N"], w["n"], w["tc"]
+    bc = N // tc
+    seed = w["seed"] + d.rank  # each rank solves its own batch (weak scaling)
+    log("[bench] generating %d x %dx%d seed %d" % (N, n, n, seed))
+    rA, iA = workloads.gaussian_soa(N, n, seed, tc)
+    dAr = torch.from_numpy(rA).cuda()
+    dAi = torch.from_numpy(iA).cuda()
+    dEr = torch.empty(N * n, dtype=torch.float64, device="cuda")
+    dEi = torch.empty_like(dEr)
+    dVr = torch.empty_like(dAr)
+    dVi = torch.empty_like(dAi)
+    st = torch.zeros(N, dtype=torch.int32, device="cuda")
+    sw = torch.zeros(N, dtype=torch.int32, device="cuda")
+    opt = ves.default_options()
+    wsp = ves.Workspace(n, bc, tc, opt)
+    stream = torch.cuda.current_stream()
+
+    def step(with_stats=False):
+        ves.eigensolve(n, bc, tc, dAr, dAi, dEr, dEi, dVr, dVi, status=st if with_stats else None,
+                       sweeps=sw if with_stats else None, options=opt, workspace=wsp, stream=stream)
+
+    peak_fp64 = ves.fp64_fma_rate(stream)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(d.local)
+    clocks.start()
+    d.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    d.barrier()
+    ms = e0.elapsed_time(e1)
+    ck = clocks.stop()
+    ms_max = d.max(ms)
+    value = N * d.world * args.steps / (ms_max * 1e-3)
+
+    # statistics + verification (outside the timed region)
+    step(with_stats=True)
+    torch.cuda.synchronize()
+    s_mean = float(sw.double().mean()) / n
+    bad_status = int((st != 0).sum())
+    ver = device_residual_check(dAr, dAi, dEr, dEi, dVr, dVi, n, tc)
+    ok = ver["max_residual"] <= RES_TOL and ver["nonfinite"] == 0 and bad_status == 0
+
+    launch_s = ms * 1e-3 / args.steps
+    achieved = N * flops_per_matrix(n, s_mean) / launch_s
+    hbm_bytes = N * (32.0 * n * n + 16.0 * n)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = read_traffic()
+
+    # e2e through the drop-in with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, rA, iA, n, bc, tc, N)
+
+    cpu = None
+    if d.rank == 0 and not args.no_cpu:
+        kind, lib = cpu_kind()
+        sample = 65_536
+        k = sample * n * n
+        cores = os.cpu_count() or 1
+        val, reps, tot = cpu_time(rA[:k].copy(), iA[:k].copy(), n, tc, cores, lib, 10.0)
+        cpu = {"value": val, "unit": "eigensolves/s", "cores": cores, "kind": kind,
+               "sample": "first %d matrices of the batch, %d repetitions (%.1f s), OpenMP over %d threads"
+                         % (sample, reps, tot, cores)}
+
+    d.done()
+    if d.rank != 0:
+        return
+    out = {
+        "metric": METRIC, "value": value, "unit": "eigensolves/s", "n_gpus": d.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: complex Gaussian N(0,1)+iN(0,1), numpy default_rng(seed 1 + rank)",
+        "config": {"workload": "1,048,576 complex128 16x16 per GPU, SoA thread_cnt=512, plain FP64 "
+                               "(zgehrd->zunghr->zlahqr->ztrevc)", "n": n, "n_matrices": N, "thread_cnt": tc,
+                   "form": "plain FP64", "l2": "inputs (4.3 GB) larger than L2; no flush",
+                   "sweeps_per_eigenvalue": s_mean},
+        "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak_fp64 / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / peak_fp64, "traffic": traffic,
+                     "peak_source": "FP64 FMA rate measured in this run (ves_fp64_fma_rate); "
+                                    "MEASURED_PEAKS.json has no FP64 figure",
+                     "flops_per_matrix": flops_per_matrix(n, s_mean),
+                     "hbm": {"achieved_gbs": hbm_bytes / launch_s / 1e9, "peak_gbs": hbm_peak,
+                             "frac": hbm_bytes / launch_s / 1e9 / hbm_peak, "bytes_per_matrix": 32 * n * n + 16 * n,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": ck,
+        "gpu_launches": args.steps,
+        "verify": dict(ver, status_nonzero=bad_status, passed=ok),
+    }
+    print(json.dumps(out), flush=True)
+    if not ok:
+        log("[bench] VERIFICATION FAILED: %s" % json.dumps(out["verify"]))
+        sys.exit(1)
+
+
+def read_traffic():
+    """DRAM bytes per launch of the fused kernel from the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "fused_fp64_gauss16.md")
+    try:
+        for ln in open(p):
+            if ln.startswith("traffic_bytes_per_launch:"):
+                return float(ln.split(":")[1])
+    except Exception:
+        pass
+    return None
+
+
+def run_e2e(args, rA, iA, n, bc, tc, N):
+    import torch
+    import ves
+    pin = lambda a: torch.from_numpy(a).pin_memory()  # noqa: E731
+    hAr0, hAi0 = pin(rA), pin(iA)
+    hAr, hAi = torch.empty_like(hAr0).pin_memory(), torch.empty_like(hAi0).pin_memory()
+    hEr = torch.empty(N * n, dtype=torch.float64).pin_memory()
+    hEi = torch.empty_like(hEr).pin_memory()
+    hVr = torch.empty_like(hAr0).pin_memory()
+    hVi = torch.empty_like(hAi0).pin_memory()
+    arr = [x.numpy() for x in (hAr, hAi, hEr, hEi, hVr, hVi)]
+    times = []
+    for it in range(args.warmup + args.steps):
+        hAr.copy_(hAr0)  # the drop-in overwrites A with T: restore the input (not timed)
+        hAi.copy_(hAi0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ves.eigensolver(n, bc, tc, *arr)
+        t1 = time.perf_counter()
+        if it >= args.warmup:
+            times.append(t1 - t0)
+    tot = sum(times)
+    h2d = 2 * N * n * n * 8
+    d2h = 2 * N * n * 8 + 4 * N * n * n * 8
+    return {"value": N * len(times) / tot, "unit": "eigensolves/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * tot / len(times),
+            "api": "eigensolver() drop-in (host pointers, pinned), synchronous"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ves", choices=["ves", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    d = Dist()
+    if args.impl == "reference":
+        run_reference_arm(args, d)
+        return
+    run_gpu_arm(args, d)
+
+
+if __name__ == "__main__":
+    main()

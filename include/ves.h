@@ -155,6 +155,12 @@ int ves_zgemv(bool hermitian, int dim, int block_cnt, int thread_cnt, const doub
 int ves_backsubstitution(int dim, int block_cnt, int thread_cnt, const double *rT, const double *iT,
                          double *rb, double *ib, void *stream);
 
+/* Measured FP64 FMA throughput of the current GPU in flop/s (an FMA counts
+ * as 2 flops): the roofline denominator of the FP64-bound solver.  Runs a
+ * few milliseconds of dependent-FMA chains on all SMs; synchronous.  No
+ * counterpart in the reference. */
+int ves_fp64_fma_rate(double *flops_per_s, void *stream);
+
 /* Last error message of the calling thread ("" if none). */
 const char *ves_last_error(void);
 /* Free the library's cached device buffers. */

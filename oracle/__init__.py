@@ -41,6 +41,9 @@ _REF_SIGS = {
     "ref_call_zgehrd": (None, [_int, _int, _int, _D, _D, _D, _D]),
     "ref_call_zunghr": (None, [_int, _int, _int, _D, _D, _D, _D]),
     "ref_hessenberg": (None, [_int, _int, _int, _D, _D, _D, _D]),
+    "ref_zgehrd_zw": (None, [_int, _int, _int, _D, _D, _D, _D]),
+    "ref_zunghr_zw": (None, [_int, _int, _int, _D, _D, _D, _D]),
+    "ref_hessenberg_zw": (None, [_int, _int, _int, _D, _D, _D, _D]),
     "ref_call_zlahqr_new": (None, [_int, _int, _int, _D, _D, _D, _D, _D, _D]),
     "ref_call_ztrevc": (None, [_int, _int, _int, _D, _D, _D, _D]),
     "ref_call_zgemv": (None, [_int, _int, _int, _int, _D, _D, _D, _D, _D, _D, _dbl, _dbl]),

@@ -500,6 +500,13 @@ int ves_backsubstitution(int dim, int block_cnt, int thread_cnt, const double *r
     return native(cuda_ok(ves::launch_backsubs(g, rT, iT, rb, ib, (cudaStream_t)stream), "backsubstitution launch"));
 }
 
+int ves_fp64_fma_rate(double *flops_per_s, void *stream)
+{
+    t_last_error.clear();
+    if (!flops_per_s) { set_error("null pointer"); return VES_ERR_ARG; }
+    return native(cuda_ok(ves::fp64_fma_rate(flops_per_s, (cudaStream_t)stream), "fp64 probe"));
+}
+
 const char *ves_last_error(void) { return t_last_error.c_str(); }
 
 void ves_release(void)

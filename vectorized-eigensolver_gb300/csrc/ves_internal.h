@@ -45,4 +45,7 @@ cudaError_t launch_zgemv(Geom g, bool herm, const double *rA, const double *iA, 
                          double rbeta, double ibeta, double *ry, double *iy, cudaStream_t st);
 cudaError_t launch_backsubs(Geom g, const double *rT, const double *iT, double *rx, double *ix, cudaStream_t st);
 
+// Measured FP64 FMA throughput of this GPU (2 flops per FMA).
+cudaError_t fp64_fma_rate(double *flops_per_s, cudaStream_t st);
+
 }  // namespace ves

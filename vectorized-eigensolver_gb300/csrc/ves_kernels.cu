@@ -209,6 +209,20 @@ __global__ void backsubs_kernel(const Geom g, const double *rT, const double *iT
     backsubs_lane<double>(g.n, T, x);
 }
 
+
+// FP64 FMA throughput probe: the roofline denominator for the FP64-bound
+// solver (a measured figure, as the HBM and tensor peaks are).  Eight
+// independent dependent-FMA chains per thread, 8 warps per SM.
+__global__ void fp64_fma_probe_kernel(double *out, int iters, double b, double c)
+{
+    double a0 = threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+        a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
 constexpr int kStageThreads = 128;
 inline unsigned stage_blocks(const Geom &g) { return (unsigned)((g.N + kStageThreads - 1) / kStageThreads); }
 
@@ -300,6 +314,34 @@ cudaError_t launch_backsubs(Geom g, const double *rT, const double *iT, double *
     if (g.N <= 0) return cudaSuccess;
     backsubs_kernel<<<stage_blocks(g), kStageThreads, 0, st>>>(g, rT, iT, rx, ix);
     return cudaGetLastError();
+}
+
+cudaError_t fp64_fma_rate(double *flops_per_s, cudaStream_t st)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int threads = 256, iters = 4096;
+    double *out = nullptr;
+    cudaError_t e = cudaMallocAsync(&out, (size_t)sms * threads * sizeof(double), st);
+    if (e != cudaSuccess) return e;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    fp64_fma_probe_kernel<<<sms, threads, 0, st>>>(out, iters, 1.0000001, 1e-9);  // warm-up
+    cudaEventRecord(e0, st);
+    const int reps = 5;
+    for (int r = 0; r < reps; ++r) fp64_fma_probe_kernel<<<sms, threads, 0, st>>>(out, iters, 1.0000001, 1e-9);
+    cudaEventRecord(e1, st);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFreeAsync(out, st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    *flops_per_s = 2.0 * 8.0 * iters * (double)sms * threads * reps / (ms * 1e-3);
+    return e;
 }
 
 }  // namespace ves

@@ -62,6 +62,7 @@ SIGNATURES = {
     "ves_ztrevc": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "ves_zgemv": (_int, [_bool, _int, _int, _int, _VP, _VP, _VP, _VP, _VP, _VP, _dbl, _dbl, _VP]),
     "ves_backsubstitution": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP, _VP]),
+    "ves_fp64_fma_rate": (_int, [_D, _VP]),
     "ves_last_error": (ctypes.c_char_p, []),
     "ves_release": (None, []),
     "ves_version": (_int, []),
@@ -302,6 +303,13 @@ def zunghr_dev(dim, block_cnt, thread_cnt, rA, iA, rtau, itau, stream=None):
 def zlahqr_dev(dim, block_cnt, thread_cnt, rE, iE, rM, iM, rS, iS, status=None, max_its=30, stream=None):
     _check(lib().ves_zlahqr(dim, block_cnt, thread_cnt, _dp(rE), _dp(iE), _dp(rM), _dp(iM), _dp(rS), _dp(iS),
                             _dp(status), max_its, _stream_ptr(stream)), "ves_zlahqr")
+
+
+def fp64_fma_rate(stream=None):
+    """Measured FP64 FMA throughput of the current GPU, flop/s."""
+    v = ctypes.c_double(0.0)
+    _check(lib().ves_fp64_fma_rate(ctypes.byref(v), _stream_ptr(stream)), "ves_fp64_fma_rate")
+    return v.value
 
 
 def ztrevc_dev(dim, block_cnt, thread_cnt, rT, iT, rR, iR, rwork, iwork, stream=None):
