@@ -116,10 +116,12 @@ enum { VES_PREC_FP64 = 0, VES_PREC_FP32_REFINE = 1 };
 enum { VES_VNORM_REFERENCE = 0, VES_VNORM_MAX = 1, VES_VNORM_TWO = 2 };
 
 typedef struct ves_options {
-    int precision;  /* VES_PREC_*; default FP64 */
-    int max_its;    /* sweeps per eigenvalue = max_its + 1; default 30 (reference Toolbox.hpp:808) */
-    int vnorm;      /* eigenvector scaling, VES_VNORM_*; default REFERENCE */
-    int reserved[8];
+    int precision;     /* VES_PREC_*; default FP64 */
+    int max_its;       /* sweeps per eigenvalue = max_its + 1; default 30 (reference Toolbox.hpp:808) */
+    int vnorm;         /* eigenvector scaling, VES_VNORM_*; default REFERENCE */
+    int refine_steps;  /* FP32_REFINE: Newton corrections per eigenpair before falling back to FP64; default 3 */
+    double refine_tol; /* FP32_REFINE: accept when ||A v - lambda v|| <= refine_tol ||A||_F ||v||; default 5e-14 */
+    int reserved[6];
 } ves_options;
 
 void ves_default_options(ves_options *opt);
@@ -127,7 +129,17 @@ void ves_default_options(ves_options *opt);
 /* Bytes of device workspace ves_eigensolve needs for this batch. */
 size_t ves_eigensolve_workspace_size(int dim, int block_cnt, int thread_cnt, const ves_options *opt);
 
-/* Full eigen-decomposition on device data.  rA/iA are read only.  rT/iT
+/* Full eigen-decomposition on device data.
+ * precision = VES_PREC_FP64: the reference path in FP64 (one launch).
+ * precision = VES_PREC_FP32_REFINE: the reference path in complex FP32, then
+ *   every eigenpair refined by Newton steps whose residual is computed in
+ *   FP64, until ||A v - lambda v|| <= refine_tol ||A||_F ||v||; a matrix that
+ *   does not get there (or whose FP32 QR hit the sweep cap, or whose data do
+ *   not fit FP32) is solved again in FP64 (status bit VES_STATUS_REFINE_FALLBACK).
+ *   Eigenvalues come in the FP32 Schur order; the REFERENCE eigenvector scaling
+ *   (unit component along the k-th Schur vector) then holds to FP32 accuracy.
+ *   rT/iT must be NULL in this mode.
+ * rA/iA are read only.  rT/iT
  * (nullable, may alias rA/iA) receive the Schur form.  status and sweeps
  * (nullable) receive one int per matrix: VES_STATUS_* bits and the number of
  * QR sweeps.  workspace may be NULL (the library then uses a cached

@@ -10,7 +10,7 @@ def dev(a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
-def run_fused(A, tc, vnorm=0, max_its=30, want_T=False, precision=0):
+def run_fused(A, tc, vnorm=0, max_its=30, want_T=False, precision=0, **opts):
     """ves_eigensolve on the complex batch A (N, n, n) in SoA layout with
     interleave tc.  Returns dict of numpy outputs (E, V, T, status, sweeps)."""
     import torch
@@ -26,7 +26,7 @@ def run_fused(A, tc, vnorm=0, max_its=30, want_T=False, precision=0):
     dTi = torch.empty_like(dAi) if want_T else None
     st = torch.full((N,), -1, dtype=torch.int32, device="cuda")
     sw = torch.full((N,), -1, dtype=torch.int32, device="cuda")
-    opt = ves.default_options(vnorm=vnorm, max_its=max_its, precision=precision)
+    opt = ves.default_options(vnorm=vnorm, max_its=max_its, precision=precision, **opts)
     ves.eigensolve(n, bc, tc, dAr, dAi, dEr, dEi, dVr, dVi, dTr, dTi, st, sw, options=opt)
     torch.cuda.synchronize()
     out = dict(

@@ -1,0 +1,157 @@
+"""Mixed-precision form (complex FP32 reduction + QR + back substitution,
+FP64 Newton refinement of every eigenpair) against the FP64 oracle.
+
+Same bar as the FP64 path: eigenvalues within 1e-12 ||A||_F of the oracle's
+after matching, residual ||A v - lambda v|| / (||A||_F ||v||) <= 1e-13 for
+every pair.  Matrices the refinement cannot certify are re-solved in FP64
+(status bit VES_STATUS_REFINE_FALLBACK).
+"""
+import numpy as np
+import pytest
+
+import oracle
+import ves
+import workloads
+from gpu_util import run_fused, soa_planes_to_batch, soa_vec_to_batch, device_residuals
+from parity import match_eigs, residuals
+
+pytestmark = pytest.mark.gpu
+MIX = ves.VES_PREC_FP32_REFINE
+
+
+def cgauss(rng, shape):
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+def oracle_E(A, tc):
+    N, n, _ = A.shape
+    rA, iA = ves.soa_from_complex(A, tc)
+    rE, iE, *_ = oracle.eigensolve(rA, iA, n, tc)
+    return ves.complex_vec_from_soa(rE, iE, n, tc)
+
+
+@pytest.mark.parametrize("n,N,tc", [(2, 64, 4), (4, 256, 32), (8, 1024, 32), (16, 2048, 512), (24, 512, 32),
+                                    (32, 512, 32), (7, 77, 7)])
+def test_mixed_matches_oracle(n, N, tc):
+    rng = np.random.default_rng(2000 + n)
+    A = cgauss(rng, (N, n, n))
+    out = run_fused(A, tc, precision=MIX)
+    nA = np.linalg.norm(A, axis=(1, 2))
+    _, err, _ = match_eigs(out["E"], oracle_E(A, tc))
+    assert (err / nA).max() <= 1e-12, (err / nA).max()
+    assert residuals(A, out["E"], out["V"]).max() <= 1e-13
+    fb = (out["status"] & ves.VES_STATUS_REFINE_FALLBACK) != 0
+    assert fb.mean() <= 0.02, fb.mean()
+    assert (out["status"] & ~ves.VES_STATUS_REFINE_FALLBACK == 0).all()
+
+
+def test_mixed_forced_fallback_equals_fp64():
+    """With no Newton step allowed nothing can be certified: every matrix goes
+    through the FP64 solver and the result is the FP64 result bit for bit."""
+    rng = np.random.default_rng(3)
+    A = cgauss(rng, (96, 10, 10))
+    fp64 = run_fused(A, 32)
+    import torch  # noqa: F401
+    out = run_fused_opts(A, 32, precision=MIX, refine_steps=0)
+    assert ((out["status"] & ves.VES_STATUS_REFINE_FALLBACK) != 0).all()
+    np.testing.assert_array_equal(out["E"], fp64["E"])
+    np.testing.assert_array_equal(out["V"], fp64["V"])
+
+
+def run_fused_opts(A, tc, **kw):
+    import torch
+    N, n, _ = A.shape
+    bc = N // tc
+    rA, iA = ves.soa_from_complex(A, tc)
+    d = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
+    dAr, dAi = d(rA), d(iA)
+    dEr = torch.empty(N * n, dtype=torch.float64, device="cuda"); dEi = torch.empty_like(dEr)
+    dVr, dVi = torch.empty_like(dAr), torch.empty_like(dAi)
+    st = torch.full((N,), -1, dtype=torch.int32, device="cuda")
+    ves.eigensolve(n, bc, tc, dAr, dAi, dEr, dEi, dVr, dVi, status=st, options=ves.default_options(**kw))
+    torch.cuda.synchronize()
+    return dict(E=ves.complex_vec_from_soa(dEr.cpu().numpy(), dEi.cpu().numpy(), n, tc),
+                V=ves.complex_from_soa(dVr.cpu().numpy(), dVi.cpu().numpy(), n, tc), status=st.cpu().numpy())
+
+
+def test_mixed_nonfinite_and_degenerate():
+    rng = np.random.default_rng(5)
+    n = 6
+    A = cgauss(rng, (64, n, n))
+    A[1] = 0
+    A[2] = np.eye(n)
+    A[3] = np.triu(rng.standard_normal((n, n)))
+    A[4, 1, 1] = np.nan
+    A[5] *= 1e30  # beyond FP32 range once squared
+    out = run_fused(A, 32, precision=MIX)
+    assert out["status"][4] & ves.VES_STATUS_NONFINITE
+    assert out["status"][5] & ves.VES_STATUS_REFINE_FALLBACK
+    good = np.ones(64, bool)
+    good[4] = False
+    assert np.isfinite(out["E"][good]).all()
+    res = residuals(A[good], out["E"][good], out["V"][good])
+    zero = np.linalg.norm(A[good], axis=(1, 2)) == 0
+    assert res[~zero].max() <= 1e-13
+
+
+def test_mixed_clustered_spectrum():
+    """Eigenvalues 1e-6 apart are below FP32 resolution: the refinement must
+    either separate them to FP64 accuracy or hand the matrix to FP64."""
+    rng = np.random.default_rng(7)
+    n, N = 8, 128
+    A = np.empty((N, n, n), complex)
+    for k in range(N):
+        c = cgauss(rng, 2)
+        lam = np.concatenate([c[0] + 1e-6 * cgauss(rng, n // 2), c[1] + 1e-6 * cgauss(rng, n // 2)])
+        X = np.eye(n) + 0.3 * cgauss(rng, (n, n))
+        A[k] = X @ np.diag(lam) @ np.linalg.inv(X)
+    out = run_fused(A, 32, precision=MIX)
+    assert residuals(A, out["E"], out["V"]).max() <= 1e-13
+    _, err, _ = match_eigs(out["E"], oracle_E(A, 32))
+    assert (err / np.linalg.norm(A, axis=(1, 2))).max() <= 1e-9  # the oracle itself is only this accurate here
+
+
+@pytest.mark.parametrize("vnorm", [0, 2])
+def test_mixed_vector_scaling(vnorm):
+    rng = np.random.default_rng(11)
+    A = cgauss(rng, (128, 12, 12))
+    ref = run_fused(A, 32, vnorm=vnorm)
+    out = run_fused(A, 32, vnorm=vnorm, precision=MIX)
+    perm, err, _ = match_eigs(out["E"], ref["E"])
+    Vm = np.take_along_axis(out["V"], perm[:, None, :], axis=2)
+    # reference scaling holds to FP32 accuracy; unit 2-norm exactly
+    ratio = np.linalg.norm(Vm, axis=1) / np.linalg.norm(ref["V"], axis=1)
+    assert np.abs(ratio - 1).max() <= (1e-4 if vnorm == 0 else 1e-14)
+
+
+@pytest.mark.slow
+def test_mixed_fullsize_n32():
+    """262,144 x 32x32 (seed 3): every pair certified on the device; eigenvalues
+    against the oracle on the first 16,384; FP64 path as the comparison."""
+    import torch
+    w = workloads.WORKLOADS["gauss32"]
+    N, n, tc = w["N"], w["n"], 512
+    rA, iA = workloads.gaussian_soa(N, n, w["seed"], tc)
+    dAr, dAi = torch.from_numpy(rA).cuda(), torch.from_numpy(iA).cuda()
+    outs = {}
+    for prec in (0, MIX):
+        dEr = torch.empty(N * n, dtype=torch.float64, device="cuda"); dEi = torch.empty_like(dEr)
+        dVr, dVi = torch.empty_like(dAr), torch.empty_like(dAi)
+        st = torch.zeros(N, dtype=torch.int32, device="cuda")
+        ves.eigensolve(n, N // tc, tc, dAr, dAi, dEr, dEi, dVr, dVi, status=st,
+                       options=ves.default_options(precision=prec))
+        torch.cuda.synchronize()
+        A = soa_planes_to_batch(dAr, dAi, n, tc)
+        res = device_residuals(A, soa_vec_to_batch(dEr, dEi, n, tc), soa_planes_to_batch(dVr, dVi, n, tc))
+        assert float(res.max()) <= 1e-13
+        outs[prec] = (dEr[: 16384 * n].cpu().numpy(), dEi[: 16384 * n].cpu().numpy(), st)
+    fb = int(((outs[MIX][2] & ves.VES_STATUS_REFINE_FALLBACK) != 0).sum())
+    assert fb <= N // 100
+    k = 16384 * n * n
+    rE, iE, *_ = oracle.eigensolve(rA[:k], iA[:k], n, tc)
+    Eo = ves.complex_vec_from_soa(rE, iE, n, tc)
+    nA = np.linalg.norm(ves.complex_from_soa(rA[:k], iA[:k], n, tc), axis=(1, 2))
+    for prec in (0, MIX):
+        E = ves.complex_vec_from_soa(outs[prec][0], outs[prec][1], n, tc)
+        _, err, _ = match_eigs(E, Eo)
+        assert (err / nA).max() <= 1e-12

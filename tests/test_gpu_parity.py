@@ -43,10 +43,11 @@ def check_against_oracle(A, tc, out, order_frac=0.98):
     assert (err / nA).max() <= EIG_TOL, (err / nA).max()
     res = residuals(A, out["E"], out["V"])
     assert res.max() <= RES_TOL, res.max()
-    # same algorithm, same shifts: the Schur order and the sweep counts agree
-    # for (almost) every matrix
+    # same algorithm, same shifts: the Schur order agrees for (almost) every
+    # matrix, and the sweep counts up to rounding-borderline deflation tests
     assert same.mean() >= order_frac, same.mean()
-    assert (out["sweeps"] == swo).mean() >= order_frac
+    assert (np.abs(out["sweeps"] - swo) <= 1).mean() >= order_frac
+    assert np.abs(out["sweeps"].mean() - swo.mean()) <= 0.05 * max(swo.mean(), 1.0)
     # eigenvectors agree up to phase where eigenvalues are separated; with the
     # reference scaling their norms agree as well
     Vm = np.take_along_axis(out["V"], perm[:, None, :], axis=2)

@@ -126,6 +126,25 @@ bool sync_ok(const char *what) { return cuda_ok(cudaDeviceSynchronize(), what); 
         if (!(ptr)) { set_error("device allocation failed"); return false; } \
     } while (0)
 
+// Workspace of ves_eigensolve: the FP64 solver's slots, and for the mixed
+// form also its FP32 slots, the fallback list and its counter (256-byte aligned).
+struct WsPlan {
+    size_t fp64, mixed, list, count, total;
+};
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+WsPlan workspace_plan(int precision, int n, long long N)
+{
+    WsPlan p{};
+    p.fp64 = align256(ves::fused_workspace_bytes(n, N, nullptr, nullptr));
+    if (precision == VES_PREC_FP32_REFINE) {
+        p.mixed = align256(ves::mixed_workspace_bytes(n, N, nullptr, nullptr));
+        p.list = align256((size_t)N * sizeof(int));
+        p.count = 256;
+    }
+    p.total = p.fp64 + p.mixed + p.list + p.count;
+    return p;
+}
+
 // ---------------------------------------------------------------------------
 // Drop-in bodies (bool: success).
 // ---------------------------------------------------------------------------
@@ -386,14 +405,18 @@ void ves_default_options(ves_options *opt)
     opt->precision = VES_PREC_FP64;
     opt->max_its = 30;
     opt->vnorm = VES_VNORM_REFERENCE;
+    opt->refine_steps = 3;
+    opt->refine_tol = 5e-14;
 }
 
 size_t ves_eigensolve_workspace_size(int dim, int block_cnt, int thread_cnt, const ves_options *opt)
 {
-    (void)opt;
     ves::Geom g;
     if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return 0;
-    return ves::fused_workspace_bytes(dim, g.N, nullptr, nullptr);
+    ves_options o;
+    ves_default_options(&o);
+    if (opt) o = *opt;
+    return workspace_plan(o.precision, dim, g.N).total;
 }
 
 int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, const double *iA, double *rE, double *iE,
@@ -408,10 +431,22 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
     ves_options o;
     ves_default_options(&o);
     if (opt) o = *opt;
-    if (o.precision != VES_PREC_FP64) { set_error("precision mode %d not available", o.precision); return VES_ERR_UNSUPPORTED; }
+    if (o.precision != VES_PREC_FP64 && o.precision != VES_PREC_FP32_REFINE) {
+        set_error("precision mode %d unknown", o.precision);
+        return VES_ERR_ARG;
+    }
+    if (o.precision == VES_PREC_FP32_REFINE && rT) {
+        set_error("the Schur form output needs precision VES_PREC_FP64");
+        return VES_ERR_UNSUPPORTED;
+    }
     if (o.max_its < 0 || o.max_its > 10000) { set_error("max_its=%d outside [0, 10000]", o.max_its); return VES_ERR_ARG; }
     if (o.vnorm < 0 || o.vnorm > 2) { set_error("vnorm=%d unknown", o.vnorm); return VES_ERR_ARG; }
-    const size_t need = ves::fused_workspace_bytes(dim, g.N, nullptr, nullptr);
+    if (o.refine_steps < 0 || o.refine_steps > 100 || !(o.refine_tol > 0.0)) {
+        set_error("refine_steps=%d / refine_tol=%g out of range", o.refine_steps, o.refine_tol);
+        return VES_ERR_ARG;
+    }
+    const WsPlan plan = workspace_plan(o.precision, dim, g.N);
+    const size_t need = plan.total;
     void *ws = workspace;
     std::unique_lock<std::mutex> lk;
     if (!ws) {
@@ -432,7 +467,31 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
     a.ws = ws;
     a.max_its = o.max_its;
     a.vnorm = o.vnorm;
-    return native(cuda_ok(ves::launch_fused_fp64(a, (cudaStream_t)stream), "eigensolve kernel launch"));
+    cudaStream_t st = (cudaStream_t)stream;
+    if (o.precision == VES_PREC_FP64)
+        return native(cuda_ok(ves::launch_fused_fp64(a, st), "eigensolve kernel launch"));
+
+    char *base = static_cast<char *>(ws);
+    int *list = reinterpret_cast<int *>(base + plan.fp64 + plan.mixed);
+    int *count = reinterpret_cast<int *>(base + plan.fp64 + plan.mixed + plan.list);
+    if (!cuda_ok(cudaMemsetAsync(count, 0, sizeof(int), st), "fallback counter reset")) return VES_ERR_CUDA;
+    ves::MixedArgs m{};
+    m.g = g;
+    m.rA = rA; m.iA = iA;
+    m.rE = rE; m.iE = iE;
+    m.rV = rV; m.iV = iV;
+    m.status = status; m.sweeps = sweeps;
+    m.ws = base + plan.fp64;
+    m.max_its = o.max_its;
+    m.vnorm = o.vnorm;
+    m.max_steps = o.refine_steps;
+    m.tol = o.refine_tol;
+    m.fb_list = list;
+    m.fb_count = count;
+    if (!cuda_ok(ves::launch_mixed(m, st), "mixed-precision kernel launch")) return VES_ERR_CUDA;
+    a.list = list;
+    a.list_count = count;
+    return native(cuda_ok(ves::launch_fused_fp64(a, st), "fallback kernel launch"));
 }
 
 int ves_zgehrd(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau, void *stream)

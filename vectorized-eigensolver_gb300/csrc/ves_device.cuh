@@ -83,10 +83,12 @@ template <class R> struct lim;
 template <> struct lim<double> {
     static __device__ __forceinline__ double eps() { return DBL_EPSILON; }
     static __device__ __forceinline__ double tiny() { return DBL_MIN; }
+    static __device__ __forceinline__ double huge() { return DBL_MAX; }
 };
 template <> struct lim<float> {
     static __device__ __forceinline__ float eps() { return FLT_EPSILON; }
     static __device__ __forceinline__ float tiny() { return FLT_MIN; }
+    static __device__ __forceinline__ float huge() { return FLT_MAX; }
 };
 
 // ---------------------------------------------------------------------------
@@ -461,7 +463,47 @@ __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool va
 // shifted diagonal T(k,k) - T(ki,ki), clamped to smin as in the reference, is
 // formed on the fly, so T is read only.  x is held in the work vector `x`.
 // Eigenvector ki comes out as R * [x; 1; 0], the reference's scaling.
+//
+// Overflow guard: the reference's back substitution has none (it omits the
+// scaled solver zlatrs that LAPACK's ztrevc uses), so a defective T -- a
+// Jordan block, whose shifted diagonal is clamped to smin ~ 1e-291 -- gives
+// Inf/NaN vectors.  Here, whenever an entry of x would exceed `big`, the
+// whole vector, including its unit entry, is scaled down; the result is then
+// R * [s x; s; 0] for some 0 < s < 1, still an eigenvector.  When no entry
+// gets that large (every well-posed case), s = 1 and the arithmetic is the
+// reference's.
 // ---------------------------------------------------------------------------
+template <class R> struct trevc_lim;
+template <> struct trevc_lim<double> { static __device__ __forceinline__ double big() { return 1e150; } };
+template <> struct trevc_lim<float> { static __device__ __forceinline__ float big() { return 1e15f; } };
+
+// Back substitution for column ki of the T-eigenvector matrix, in x(1:ki-1);
+// returns the scale s of the unit entry.
+template <class R, class MT, class V>
+__device__ __forceinline__ R trevc_solve(const int ki, const MT &T, const V &x, const R smin, const cx<R> tkk)
+{
+    const R big = trevc_lim<R>::big();
+    R s = R(1);
+    for (int k = 1; k <= ki - 1; ++k) { const cx<R> v = T.ld(k, ki); x.st(k, mk(-v.r, -v.i)); }
+    for (int j = ki - 1; j >= 1; --j) {
+        cx<R> d = csub(T.ld(j, j), tkk);
+        if (cabs1(d) < smin) d = mk(smin, R(0));
+        cx<R> xj = x.ld(j);
+        const R num = cabs1(xj), den = cabs1(d);
+        if (num > big * den) {
+            // x(j)/d would exceed big: scale x(1:ki-1) and the unit entry so that it is big
+            const R f = (big * den) / num;
+            for (int i = 1; i <= ki - 1; ++i) x.st(i, cscal(x.ld(i), f));
+            xj = cscal(xj, f);
+            s *= f;
+        }
+        xj = cdiv(xj, d);
+        x.st(j, xj);
+        for (int i = j - 1; i >= 1; --i) x.st(i, csub(x.ld(i), cmul(T.ld(i, j), xj)));
+    }
+    return s;
+}
+
 template <class R, class MT, class MR, class V>
 __device__ void ztrevc_lane(const int n, const MT &T, const MR &Rm, const V &x)
 {
@@ -470,18 +512,12 @@ __device__ void ztrevc_lane(const int n, const MT &T, const MR &Rm, const V &x)
     for (int ki = n; ki >= 2; --ki) {
         const cx<R> tkk = T.ld(ki, ki);
         const R smin = fmax(ulp * cabs1(tkk), smlnum);
-        for (int k = 1; k <= ki - 1; ++k) { const cx<R> v = T.ld(k, ki); x.st(k, mk(-v.r, -v.i)); }
         // back substitution with (T(1:ki-1,1:ki-1) - T(ki,ki) I)
-        for (int j = ki - 1; j >= 1; --j) {
-            cx<R> d = csub(T.ld(j, j), tkk);
-            if (cabs1(d) < smin) d = mk(smin, R(0));
-            const cx<R> xj = cdiv(x.ld(j), d);
-            x.st(j, xj);
-            for (int i = j - 1; i >= 1; --i) x.st(i, csub(x.ld(i), cmul(T.ld(i, j), xj)));
-        }
-        // R(:, ki) := R(:, 1:ki-1) x + R(:, ki)
+        const R s = trevc_solve<R>(ki, T, x, smin, tkk);
+        // R(:, ki) := R(:, 1:ki-1) x + s R(:, ki)
         for (int i = 1; i <= n; ++i) {
             cx<R> acc = Rm.ld(i, ki);
+            if (s != R(1)) acc = cscal(acc, s);
             for (int j = 1; j <= ki - 1; ++j) acc = cadd(acc, cmul(Rm.ld(i, j), x.ld(j)));
             Rm.st(i, ki, acc);
         }

@@ -26,7 +26,30 @@ struct FusedArgs {
     void *ws;               // workspace
     int max_its;
     int vnorm;
+    // optional index list: solve only matrices list[0 .. *list_count) (the
+    // mixed-precision form's fallback pass); status gets ST_REFINE_FALLBACK
+    const int *list;
+    const int *list_count;
 };
+
+struct MixedArgs {
+    Geom g;
+    const double *rA, *iA;
+    double *rE, *iE;
+    double *rV, *iV;
+    int *status;
+    int *sweeps;
+    void *ws;
+    int max_its;
+    int vnorm;
+    int max_steps;  // Newton corrections per eigenpair
+    double tol;     // ||r|| <= tol ||A||_F ||v||
+    int *fb_list;   // matrices handed to the FP64 solver
+    int *fb_count;
+};
+
+size_t mixed_workspace_bytes(int n, long long N, int *out_blocks, int *out_threads);
+cudaError_t launch_mixed(const MixedArgs &a, cudaStream_t st);
 
 // Fused zgehrd -> zunghr -> zlahqr -> ztrevc, FP64.
 size_t fused_workspace_bytes(int n, long long N, int *out_blocks, int *out_threads);

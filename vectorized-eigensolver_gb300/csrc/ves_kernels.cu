@@ -62,7 +62,8 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
     const int lane = threadIdx.x & 31;
     const long long slot = (long long)blockIdx.x * (kFusedThreads / 32) + (threadIdx.x >> 5);
     const long long nslots = (long long)gridDim.x * (kFusedThreads / 32);
-    const long long ngroups = (N + 31) / 32;
+    const long long Nw = a.list ? (long long)*a.list_count : N;
+    const long long ngroups = (Nw + 31) / 32;
     const long long per_lane = 2LL * n * n + n;  // H, Z, work vector
 
     double2 *base = reinterpret_cast<double2 *>(a.ws) + slot * per_lane * 32 + lane;
@@ -71,8 +72,9 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
     const VecIlv<double> W{base + 2LL * n * n * 32};
 
     for (long long g = slot; g < ngroups; g += nslots) {
-        const long long m = g * 32 + lane;
-        const bool valid = m < N;
+        const long long idx = g * 32 + lane;
+        const bool valid = idx < Nw;
+        const long long m = valid ? (a.list ? (long long)a.list[idx] : idx) : 0;
         const long long mo = valid ? soa_mat_off(m, n, tc) : 0;
         const long long vo = valid ? soa_vec_off(m, n, tc) : 0;
         int status = 0, sweeps = 0;
@@ -103,7 +105,7 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
             ztrevc_lane<double>(n, H, Z, W);
             const MatSoA<double> V{a.rV + mo, a.iV + mo, tc, n};
             write_vectors<double>(n, Z, V, a.vnorm);
-            if (a.status) a.status[m] = status;
+            if (a.status) a.status[m] = status | (a.list ? ST_REFINE_FALLBACK : 0);
             if (a.sweeps) a.sweeps[m] = sweeps;
         }
     }

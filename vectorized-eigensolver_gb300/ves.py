@@ -34,7 +34,8 @@ class VesError(RuntimeError):
 
 
 class Options(ctypes.Structure):
-    _fields_ = [("precision", _int), ("max_its", _int), ("vnorm", _int), ("reserved", _int * 8)]
+    _fields_ = [("precision", _int), ("max_its", _int), ("vnorm", _int), ("refine_steps", _int),
+                ("refine_tol", _dbl), ("reserved", _int * 6)]
 
 
 # exported symbol -> (restype, argtypes); every name declared in include/ves.h
