@@ -37,7 +37,7 @@ def run_fused(A, tc, vnorm=0, max_its=30, want_T=False, precision=0, **opts):
     if want_T:
         out["T"] = ves.complex_from_soa(dTr.cpu().numpy(), dTi.cpu().numpy(), n, tc)
     # the input is read only
-    assert np.array_equal(dAr.cpu().numpy(), rA) and np.array_equal(dAi.cpu().numpy(), iA)
+    assert np.array_equal(dAr.cpu().numpy(), rA, equal_nan=True) and np.array_equal(dAi.cpu().numpy(), iA, equal_nan=True)
     return out
 
 

@@ -117,11 +117,17 @@ def test_mixed_vector_scaling(vnorm):
     A = cgauss(rng, (128, 12, 12))
     ref = run_fused(A, 32, vnorm=vnorm)
     out = run_fused(A, 32, vnorm=vnorm, precision=MIX)
-    perm, err, _ = match_eigs(out["E"], ref["E"])
+    perm, err, same = match_eigs(out["E"], ref["E"])
     Vm = np.take_along_axis(out["V"], perm[:, None, :], axis=2)
-    # reference scaling holds to FP32 accuracy; unit 2-norm exactly
     ratio = np.linalg.norm(Vm, axis=1) / np.linalg.norm(ref["V"], axis=1)
-    assert np.abs(ratio - 1).max() <= (1e-4 if vnorm == 0 else 1e-14)
+    if vnorm == 2:
+        assert np.abs(ratio - 1).max() <= 1e-14
+    else:
+        # the reference scaling (unit component along the k-th Schur vector)
+        # depends on the Schur order; where the FP32 QR deflated in the same
+        # order as the FP64 QR it holds to FP32 accuracy
+        assert same.mean() >= 0.9
+        assert np.abs(ratio[same] - 1).max() <= 1e-4
 
 
 @pytest.mark.slow

@@ -261,10 +261,15 @@ def test_dropin_zlahqr_ztrevc_vs_reference(gold):
         T = ves.complex_from_soa(rH, iH, n, tc)
         S = ves.complex_from_soa(rS, iS, n, tc)
         Tref = ves.complex_from_soa(gold[c + "/zlahqr_rT"], gold[c + "/zlahqr_iT"], n, tc)
-        Sref = ves.complex_from_soa(gold[c + "/zlahqr_rS"], gold[c + "/zlahqr_iS"], n, tc)
-        np.testing.assert_allclose(T, Tref, atol=1e-12 * s.max())
-        # the reference's CPU path starts S at i*I (utils.cpp:169); here S starts at I
-        np.testing.assert_allclose(1j * S, Sref, atol=1e-12 * n)
+        # A Schur form is unique only up to a diagonal unitary similarity, and
+        # this algorithm fixes those phases from subdiagonals that have
+        # converged to rounding level ("make H(I,I-1) real"), so two correct
+        # implementations that round differently differ by such phases.
+        # Compare the invariants: |T|, S unitary, S T S^H = M.
+        assert np.abs(np.tril(T, -1)).max() == 0.0
+        np.testing.assert_allclose(np.abs(T), np.abs(Tref), atol=1e-11 * s.max())
+        assert _unitary_err(S) <= 1e-13 * n
+        assert np.abs(S @ T @ np.conj(np.swapaxes(S, 1, 2)) - H0).max() <= 1e-13 * s.max()
         # ztrevc on the reference's own (T, S): same algorithm, same inputs
         rT, iT = gold[c + "/zlahqr_rT"].copy(), gold[c + "/zlahqr_iT"].copy()
         rR, iR = gold[c + "/zlahqr_rS"].copy(), gold[c + "/zlahqr_iS"].copy()
