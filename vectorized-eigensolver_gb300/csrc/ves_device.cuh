@@ -44,6 +44,41 @@ template <class R> __device__ __forceinline__ cx<R> csub(cx<R> a, cx<R> b) { ret
 template <class R> __device__ __forceinline__ cx<R> cscal(cx<R> a, R d) { return mk(a.r * d, a.i * d); }
 template <class R> __device__ __forceinline__ cx<R> conj(cx<R> a) { return mk(a.r, -a.i); }
 
+// Multiply-accumulate forms written as explicit FMAs: 4 FMAs per complex
+// multiply-add instead of the 6 instructions (MUL, FMA, ADD per component)
+// that contraction leaves when the sum is written s + a*b.  On GB300 every
+// FP64 instruction costs the same pipe time, so this is the instruction count
+// that bounds the solver.
+template <class R> __device__ __forceinline__ cx<R> cmac(cx<R> s, cx<R> a, cx<R> b)  // s + a*b
+{
+    return mk(fma(-a.i, b.i, fma(a.r, b.r, s.r)), fma(a.r, b.i, fma(a.i, b.r, s.i)));
+}
+template <class R> __device__ __forceinline__ cx<R> cnmac(cx<R> s, cx<R> a, cx<R> b)  // s - a*b
+{
+    return mk(fma(a.i, b.i, fma(-a.r, b.r, s.r)), fma(-a.r, b.i, fma(-a.i, b.r, s.i)));
+}
+template <class R> __device__ __forceinline__ cx<R> cmacc(cx<R> s, cx<R> a, cx<R> b)  // s + a*conj(b)
+{
+    return mk(fma(a.i, b.i, fma(a.r, b.r, s.r)), fma(-a.r, b.i, fma(a.i, b.r, s.i)));
+}
+template <class R> __device__ __forceinline__ cx<R> cnmacc(cx<R> s, cx<R> a, cx<R> b)  // s - a*conj(b)
+{
+    return mk(fma(-a.i, b.i, fma(-a.r, b.r, s.r)), fma(a.r, b.i, fma(-a.i, b.r, s.i)));
+}
+template <class R> __device__ __forceinline__ cx<R> cjmac(cx<R> s, cx<R> a, cx<R> b)  // s + conj(a)*b
+{
+    return mk(fma(a.i, b.i, fma(a.r, b.r, s.r)), fma(-a.i, b.r, fma(a.r, b.i, s.i)));
+}
+// Apply a 2-element reflector to the pair (h1, h2): z = c1*h1 + t2*h2,
+// h1 -= z, h2 -= z*w (12 FP64 instructions).  Rows use c1 = conj(tau), w = v;
+// columns use c1 = tau, w = conj(v).
+template <class R> __device__ __forceinline__ void rot_pair(cx<R> &h1, cx<R> &h2, const cx<R> c1, const R t2, const cx<R> w)
+{
+    const cx<R> z = mk(fma(t2, h2.r, fma(c1.r, h1.r, -c1.i * h1.i)), fma(t2, h2.i, fma(c1.r, h1.i, c1.i * h1.r)));
+    h1 = csub(h1, z);
+    h2 = cnmac(h2, z, w);
+}
+
 // 1/z and a/b by Smith's method (the reference's ComplexDouble.hpp:283-353 semantics).
 template <class R> __device__ __forceinline__ cx<R> cinv(cx<R> z)
 {
@@ -158,7 +193,7 @@ __device__ void zgehrd_lane(const int n, const M &A, const V &tau)
         R xnorm2 = R(0);
         for (int k = i + 2; k <= n; ++k) {
             cx<R> x = A.ld(k, i);
-            xnorm2 += x.r * x.r + x.i * x.i;
+            xnorm2 = fma(x.i, x.i, fma(x.r, x.r, xnorm2));
         }
         const bool trivial = (xnorm2 == R(0)) && (alpha.i == R(0));
         const R beta = trivial ? alpha.r : -copysign(sqrt(alpha.r * alpha.r + alpha.i * alpha.i + xnorm2), alpha.r);
@@ -174,19 +209,19 @@ __device__ void zgehrd_lane(const int n, const M &A, const V &tau)
         // v = [1; A(i+2:n, i)].  Right: A(1:n, i+1:n) -= tau * (A v) v^H, row by row.
         for (int k = 1; k <= n; ++k) {
             cx<R> s = A.ld(k, i + 1);
-            for (int j = 2; j <= m; ++j) s = cadd(s, cmul(A.ld(k, i + j), A.ld(i + j, i)));
+            for (int j = 2; j <= m; ++j) s = cmac(s, A.ld(k, i + j), A.ld(i + j, i));
             const cx<R> ts = cmul(t, s);
             A.st(k, i + 1, csub(A.ld(k, i + 1), ts));
-            for (int j = 2; j <= m; ++j) A.st(k, i + j, csub(A.ld(k, i + j), cmulc(ts, A.ld(i + j, i))));
+            for (int j = 2; j <= m; ++j) A.st(k, i + j, cnmacc(A.ld(k, i + j), ts, A.ld(i + j, i)));
         }
         // Left: A(i+1:n, i+1:n) -= conj(tau) * v (v^H A), column by column.
         const cx<R> tc = conj(t);
         for (int j = i + 1; j <= n; ++j) {
             cx<R> s = A.ld(i + 1, j);
-            for (int k = 2; k <= m; ++k) s = cadd(s, cjmul(A.ld(i + k, i), A.ld(i + k, j)));
+            for (int k = 2; k <= m; ++k) s = cjmac(s, A.ld(i + k, i), A.ld(i + k, j));
             const cx<R> ts = cmul(tc, s);
             A.st(i + 1, j, csub(A.ld(i + 1, j), ts));
-            for (int k = 2; k <= m; ++k) A.st(i + k, j, csub(A.ld(i + k, j), cmul(A.ld(i + k, i), ts)));
+            for (int k = 2; k <= m; ++k) A.st(i + k, j, cnmac(A.ld(i + k, j), A.ld(i + k, i), ts));
         }
         A.st(i + 1, i, mk(beta, R(0)));
     }
@@ -213,10 +248,10 @@ __device__ void zunghr_lane(const int n, const MA &A, const MQ &Q, const V &tau)
         // apply H(i) from the left to Q(c:n, c+1:n): Q -= tau * u (u^H Q)
         for (int j = c + 1; j <= n; ++j) {
             cx<R> s = Q.ld(c, j);
-            for (int k = c + 1; k <= n; ++k) s = cadd(s, cjmul(A.ld(k, i), Q.ld(k, j)));
+            for (int k = c + 1; k <= n; ++k) s = cjmac(s, A.ld(k, i), Q.ld(k, j));
             const cx<R> ts = cmul(t, s);
             Q.st(c, j, csub(Q.ld(c, j), ts));
-            for (int k = c + 1; k <= n; ++k) Q.st(k, j, csub(Q.ld(k, j), cmul(A.ld(k, i), ts)));
+            for (int k = c + 1; k <= n; ++k) Q.st(k, j, cnmac(Q.ld(k, j), A.ld(k, i), ts));
         }
         // column c: -tau * u below, 1 - tau on the diagonal, zeros above
         const cx<R> mt = mk(-t.r, -t.i);
@@ -415,29 +450,31 @@ __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool va
             const R t2 = t1.r * w1.r - t1.i * w1.i;
             if (act) {
                 // rows K, K+1, columns K..n (wantT: I2 = n)
+                const cx<R> c1 = conj(t1);
                 for (int j = K; j <= n; ++j) {
-                    const cx<R> h1 = H.ld(K, j), h2 = H.ld(K + 1, j);
-                    const cx<R> z = cadd(cmulc(h1, t1), cscal(h2, t2));
-                    H.st(K, j, csub(h1, z));
-                    H.st(K + 1, j, csub(h2, cmul(z, w1)));
+                    cx<R> h1 = H.ld(K, j), h2 = H.ld(K + 1, j);
+                    rot_pair(h1, h2, c1, t2, w1);
+                    H.st(K, j, h1);
+                    H.st(K + 1, j, h2);
                 }
             }
             // columns K, K+1, rows 1..min(K+2, I)
             const int je = (K + 2) < n ? (K + 2) : n;
             for (int j = 1; j <= je; ++j) {
                 if (act && j <= I) {
-                    const cx<R> h1 = H.ld(j, K), h2 = H.ld(j, K + 1);
-                    const cx<R> z = cadd(cmul(h1, t1), cscal(h2, t2));
-                    H.st(j, K, csub(h1, z));
-                    H.st(j, K + 1, csub(h2, cmulc(z, w1)));
+                    cx<R> h1 = H.ld(j, K), h2 = H.ld(j, K + 1);
+                    rot_pair(h1, h2, t1, t2, conj(w1));
+                    H.st(j, K, h1);
+                    H.st(j, K + 1, h2);
                 }
             }
             if (act) {
+                const cx<R> cw = conj(w1);
                 for (int j = 1; j <= n; ++j) {
-                    const cx<R> z1 = Z.ld(j, K), z2 = Z.ld(j, K + 1);
-                    const cx<R> z = cadd(cmul(z1, t1), cscal(z2, t2));
-                    Z.st(j, K, csub(z1, z));
-                    Z.st(j, K + 1, csub(z2, cmulc(z, w1)));
+                    cx<R> z1 = Z.ld(j, K), z2 = Z.ld(j, K + 1);
+                    rot_pair(z1, z2, t1, t2, cw);
+                    Z.st(j, K, z1);
+                    Z.st(j, K + 1, z2);
                 }
             }
         }
@@ -499,7 +536,7 @@ __device__ __forceinline__ R trevc_solve(const int ki, const MT &T, const V &x, 
         }
         xj = cdiv(xj, d);
         x.st(j, xj);
-        for (int i = j - 1; i >= 1; --i) x.st(i, csub(x.ld(i), cmul(T.ld(i, j), xj)));
+        for (int i = j - 1; i >= 1; --i) x.st(i, cnmac(x.ld(i), T.ld(i, j), xj));
     }
     return s;
 }
@@ -518,7 +555,7 @@ __device__ void ztrevc_lane(const int n, const MT &T, const MR &Rm, const V &x)
         for (int i = 1; i <= n; ++i) {
             cx<R> acc = Rm.ld(i, ki);
             if (s != R(1)) acc = cscal(acc, s);
-            for (int j = 1; j <= ki - 1; ++j) acc = cadd(acc, cmul(Rm.ld(i, j), x.ld(j)));
+            for (int j = 1; j <= ki - 1; ++j) acc = cmac(acc, Rm.ld(i, j), x.ld(j));
             Rm.st(i, ki, acc);
         }
     }

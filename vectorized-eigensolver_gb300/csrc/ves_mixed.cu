@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kMixedThreads) fused_mixed_kernel(const MixedA
             for (int k = 1; k <= n; ++k)
                 for (int i = 1; i <= n; ++i) {
                     cx<float> acc = mk(0.f, 0.f);
-                    for (int j = 1; j <= k; ++j) acc = cadd(acc, cmul(Z.ld(i, j), X.ld(j, k)));
+                    for (int j = 1; j <= k; ++j) acc = cmac(acc, Z.ld(i, j), X.ld(j, k));
                     V.st(i, k, up(acc));
                 }
         }
@@ -146,9 +146,9 @@ __global__ void __launch_bounds__(kMixedThreads) fused_mixed_kernel(const MixedA
                 for (int i = 1; i <= n; ++i) {
                     const cx<double> vi = V.ld(i, k);
                     cx<double> acc = mk(-(lam.r * vi.r - lam.i * vi.i), -(lam.r * vi.i + lam.i * vi.r));
-                    for (int j = 1; j <= n; ++j) acc = cadd(acc, cmul(A.ld(i, j), V.ld(j, k)));
-                    rn2 += acc.r * acc.r + acc.i * acc.i;
-                    vn2 += vi.r * vi.r + vi.i * vi.i;
+                    for (int j = 1; j <= n; ++j) acc = cmac(acc, A.ld(i, j), V.ld(j, k));
+                    rn2 = fma(acc.i, acc.i, fma(acc.r, acc.r, rn2));
+                    vn2 = fma(vi.i, vi.i, fma(vi.r, vi.r, vn2));
                     r32.st(i, down(acc));
                 }
                 if (rn2 <= tol2 * (double)nA2 * vn2) { act = false; continue; }
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(kMixedThreads) fused_mixed_kernel(const MixedA
                 // FP32 correction through the Schur form
                 for (int i = 1; i <= n; ++i) {
                     cx<float> s = mk(0.f, 0.f);
-                    for (int j = 1; j <= n; ++j) s = cadd(s, cjmul(Z.ld(j, i), r32.ld(j)));
+                    for (int j = 1; j <= n; ++j) s = cjmac(s, Z.ld(j, i), r32.ld(j));
                     rp.st(i, s);
                 }
                 const cx<float> l32 = down(lam);
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(kMixedThreads) fused_mixed_kernel(const MixedA
                 for (int i = n; i >= 1; --i) {
                     cx<float> s = rp.ld(i);
                     s = mk(-s.r, -s.i);
-                    for (int j = i + 1; j <= n; ++j) s = csub(s, cmul(T.ld(i, j), dx.ld(j)));
+                    for (int j = i + 1; j <= n; ++j) s = cnmac(s, T.ld(i, j), dx.ld(j));
                     if (i == k) {  // dlambda x_k = r'_k + sum_{j>k} T_kj dx_j = -s
                         dl = cscal(mk(-s.r, -s.i), 1.f / X.ld(k, k).r);
                         dx.st(i, mk(0.f, 0.f));
@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(kMixedThreads) fused_mixed_kernel(const MixedA
                 }
                 for (int i = 1; i <= n; ++i) {
                     cx<float> s = mk(0.f, 0.f);
-                    for (int j = 1; j <= n; ++j) s = cadd(s, cmul(Z.ld(i, j), dx.ld(j)));
+                    for (int j = 1; j <= n; ++j) s = cmac(s, Z.ld(i, j), dx.ld(j));
                     V.st(i, k, cadd(V.ld(i, k), up(s)));
                 }
                 lam = cadd(lam, up(dl));
