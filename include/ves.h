@@ -173,6 +173,28 @@ int ves_backsubstitution(int dim, int block_cnt, int thread_cnt, const double *r
  * counterpart in the reference. */
 int ves_fp64_fma_rate(double *flops_per_s, void *stream);
 
+/* Allocation-free variant of ves_eigensolve (FP64, reference eigenvector
+ * scaling, no Schur-form or sweep output).  No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory: hosts whose allocator is
+ * owned by someone else, code that may not allocate (or let the driver
+ * synchronise) after start-up.  It calls no cudaMalloc, cudaFree or other
+ * allocating routine; its scratch space is a static device array of
+ * VES_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * process exit.  The caller passes the inputs and outputs (device pointers,
+ * layout as ves_eigensolve).  dim must not exceed VES_NOALLOC_MAX_DIM;
+ * larger dims return VES_ERR_ARG with a message in ves_last_error().
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current: make that first call
+ * before any stream capture.  All calls on a device share the array, so calls
+ * that overlap on the GPU race and must be serialised by the caller.
+ * Asynchronous on `stream`. */
+#define VES_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
+#define VES_NOALLOC_MAX_DIM 64
+int ves_eigensolve_noalloc(int dim, int block_cnt, int thread_cnt,
+                           const double *rA, const double *iA, double *rE, double *iE, double *rV, double *iV,
+                           int *status, void *stream);
+
 /* Last error message of the calling thread ("" if none). */
 const char *ves_last_error(void);
 /* Free the library's cached device buffers. */

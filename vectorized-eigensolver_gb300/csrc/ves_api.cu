@@ -316,6 +316,10 @@ int native(bool ok) { return ok ? VES_OK : (t_last_error.find("alloc") != std::s
 
 }  // namespace
 
+namespace ves {
+void set_error_message(const char *msg) { t_last_error = msg ? msg : ""; }
+}  // namespace ves
+
 extern "C" {
 
 // ------------------------------- drop-in ----------------------------------

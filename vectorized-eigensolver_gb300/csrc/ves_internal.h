@@ -68,6 +68,13 @@ cudaError_t launch_zgemv(Geom g, bool herm, const double *rA, const double *iA, 
                          double rbeta, double ibeta, double *ry, double *iy, cudaStream_t st);
 cudaError_t launch_backsubs(Geom g, const double *rT, const double *iT, double *rx, double *ix, cudaStream_t st);
 
+// The FP64 fused kernel on a caller-chosen grid of `blocks` x 4 warps; the
+// workspace must hold blocks * 4 warp slots.
+cudaError_t launch_fused_fp64_blocks(const FusedArgs &a, int blocks, cudaStream_t st);
+
+// Record the calling thread's message for ves_last_error().
+void set_error_message(const char *msg);
+
 // Measured FP64 FMA throughput of this GPU (2 flops per FMA).
 cudaError_t fp64_fma_rate(double *flops_per_s, cudaStream_t st);
 

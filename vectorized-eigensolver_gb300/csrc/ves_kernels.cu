@@ -265,6 +265,13 @@ cudaError_t launch_fused_fp64(const FusedArgs &a, cudaStream_t st)
     return cudaGetLastError();
 }
 
+cudaError_t launch_fused_fp64_blocks(const FusedArgs &a, int blocks, cudaStream_t st)
+{
+    if (a.g.N <= 0) return cudaSuccess;
+    fused_fp64_kernel<<<blocks, kFusedThreads, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_zgehrd(Geom g, double *rA, double *iA, double *rtau, double *itau, cudaStream_t st)
 {
     if (g.N <= 0) return cudaSuccess;

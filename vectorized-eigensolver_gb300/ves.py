@@ -64,6 +64,7 @@ SIGNATURES = {
     "ves_zgemv": (_int, [_bool, _int, _int, _int, _VP, _VP, _VP, _VP, _VP, _VP, _dbl, _dbl, _VP]),
     "ves_backsubstitution": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP, _VP]),
     "ves_fp64_fma_rate": (_int, [_D, _VP]),
+    "ves_eigensolve_noalloc": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "ves_last_error": (ctypes.c_char_p, []),
     "ves_release": (None, []),
     "ves_version": (_int, []),
