@@ -220,6 +220,52 @@ def device_residual_check(dAr, dAi, dEr, dEi, dVr, dVi, n, tc, chunk=1 << 17):
     return {"max_residual": worst, "nonfinite": nonfinite, "checked_matrices": int(A.shape[0])}
 
 
+def measure_form(name, n, N, seed, tc, precision, warmup, steps):
+    """Device-resident eigensolves/s of one form on one seeded Gaussian batch,
+    verified on the device afterwards (every residual)."""
+    import torch
+    import ves
+    import workloads
+    bc = N // tc
+    rA, iA = workloads.gaussian_soa(N, n, seed, tc)
+    dAr, dAi = torch.from_numpy(rA).cuda(), torch.from_numpy(iA).cuda()
+    del rA, iA
+    dEr = torch.empty(N * n, dtype=torch.float64, device="cuda")
+    dEi = torch.empty_like(dEr)
+    dVr, dVi = torch.empty_like(dAr), torch.empty_like(dAi)
+    st = torch.zeros(N, dtype=torch.int32, device="cuda")
+    sw = torch.zeros(N, dtype=torch.int32, device="cuda")
+    opt = ves.default_options(precision=precision)
+    wsp = ves.Workspace(n, bc, tc, opt)
+    stream = torch.cuda.current_stream()
+    run = lambda **kw: ves.eigensolve(n, bc, tc, dAr, dAi, dEr, dEi, dVr, dVi, options=opt, workspace=wsp,  # noqa: E731
+                                      stream=stream, **kw)
+    for _ in range(warmup):
+        run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    run(status=st, sweeps=sw)
+    torch.cuda.synchronize()
+    ver = device_residual_check(dAr, dAi, dEr, dEi, dVr, dVi, n, tc)
+    fb = int(((st & 8) != 0).sum())
+    other = int(((st & ~8) != 0).sum())
+    out = {"form": name, "n": n, "n_matrices": N, "seed": seed, "value": N / (ms * 1e-3), "unit": "eigensolves/s",
+           "ms_per_step": ms, "steps": steps, "warmup": warmup, "sweeps_per_eigenvalue": float(sw.double().mean()) / n,
+           "max_residual": ver["max_residual"], "nonfinite": ver["nonfinite"], "status_other": other,
+           "passed": ver["max_residual"] <= RES_TOL and ver["nonfinite"] == 0 and other == 0}
+    if precision:
+        out["fp64_fallback_matrices"] = fb
+    del dAr, dAi, dEr, dEi, dVr, dVi, wsp
+    torch.cuda.empty_cache()
+    return out
+
+
 def flops_per_matrix(n, s):
     return 24.0 * n ** 3 + 20.0 * s * n ** 3
 
@@ -308,6 +354,16 @@ def run_gpu_arm(args, d):
                "sample": "first %d matrices of the batch, %d repetitions (%.1f s), OpenMP over %d threads"
                          % (sample, reps, tot, cores)}
 
+    forms = []
+    if d.world == 1 and not args.no_forms:
+        forms.append(dict(measure_form("FP32+refine", n, N, w["seed"], tc, 1, 2, args.steps),
+                          speedup_vs_plain=None))
+        forms[-1]["speedup_vs_plain"] = forms[-1]["value"] / value
+        p32 = measure_form("plain FP64", 32, 262_144, 3, 512, 0, 1, 2)
+        m32 = measure_form("FP32+refine", 32, 262_144, 3, 512, 1, 1, 2)
+        m32["speedup_vs_plain"] = m32["value"] / p32["value"]
+        forms += [p32, m32]
+
     d.done()
     if d.rank != 0:
         return
@@ -333,10 +389,11 @@ def run_gpu_arm(args, d):
         "clocks": ck,
         "gpu_launches": args.steps,
         "verify": dict(ver, status_nonzero=bad_status, passed=ok),
+        "forms": forms,
     }
     print(json.dumps(out), flush=True)
-    if not ok:
-        log("[bench] VERIFICATION FAILED: %s" % json.dumps(out["verify"]))
+    if not ok or not all(f["passed"] for f in forms):
+        log("[bench] VERIFICATION FAILED: %s" % json.dumps([out["verify"]] + forms))
         sys.exit(1)
 
 
@@ -381,6 +438,26 @@ def run_e2e(args, rA, iA, n, bc, tc, N):
             "api": "eigensolver() drop-in (host pointers, pinned), synchronous"}
 
 
+def run_ncu_case(args):
+    """One solve per form on a small batch (inputs still larger than L2), no
+    timing: the case the ncu captures under profiles/ are taken on."""
+    import torch
+    import ves
+    n, N, tc = args.ncu_n, args.ncu_case, 512
+    g = torch.Generator(device="cuda").manual_seed(1)
+    rA = torch.randn(N * n * n, dtype=torch.float64, device="cuda", generator=g)
+    iA = torch.randn(N * n * n, dtype=torch.float64, device="cuda", generator=g)
+    rE = torch.empty(N * n, dtype=torch.float64, device="cuda")
+    iE = torch.empty_like(rE)
+    rV, iV = torch.empty_like(rA), torch.empty_like(iA)
+    for prec in (0, 1):
+        opt = ves.default_options(precision=prec)
+        ws = ves.Workspace(n, N // tc, tc, opt)
+        ves.eigensolve(n, N // tc, tc, rA, iA, rE, iE, rV, iV, options=opt, workspace=ws)
+        torch.cuda.synchronize()
+    print("ncu case done: %d x %dx%d, FP64 then FP32+refine" % (N, n, n))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -389,7 +466,14 @@ def main():
     ap.add_argument("--impl", default="ves", choices=["ves", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the FP32+refine and n=32 lines")
+    ap.add_argument("--ncu-case", type=int, default=0, metavar="N",
+                    help="no benchmark: one solve per form on N matrices (for ncu captures)")
+    ap.add_argument("--ncu-n", type=int, default=16)
     args = ap.parse_args()
+    if args.ncu_case:
+        run_ncu_case(args)
+        return
     d = Dist()
     if args.impl == "reference":
         run_reference_arm(args, d)
