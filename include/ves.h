@@ -109,7 +109,8 @@ enum {
     VES_STATUS_ITCAP = 1,           /* an eigenvalue used up its sweep budget (the reference moves on silently) */
     VES_STATUS_NONFINITE = 2,       /* input held Inf/NaN; outputs are NaN */
     VES_STATUS_SHIFT_FALLBACK = 4,  /* learned shift replaced by Wilkinson's at least once */
-    VES_STATUS_REFINE_FALLBACK = 8  /* mixed precision: re-solved in FP64 */
+    VES_STATUS_REFINE_FALLBACK = 8, /* mixed precision: re-solved in FP64 */
+    VES_STATUS_BAD_DIM = 16         /* mixed-size batch: order outside [1, max_dim], not solved */
 };
 
 enum { VES_PREC_FP64 = 0, VES_PREC_FP32_REFINE = 1 };
@@ -121,7 +122,13 @@ typedef struct ves_options {
     int vnorm;         /* eigenvector scaling, VES_VNORM_*; default REFERENCE */
     int refine_steps;  /* FP32_REFINE: Newton corrections per eigenpair before falling back to FP64; default 3 */
     double refine_tol; /* FP32_REFINE: accept when ||A v - lambda v|| <= refine_tol ||A||_F ||v||; default 5e-14 */
-    int reserved[6];
+    int want_vectors;  /* 1 (default): eigenvalues and eigenvectors; 0: eigenvalues only (FP64; the QR
+                        * runs on the active block only, no Q and no Schur vectors -- the same
+                        * eigenvalues, about a third of the QR work; rV/iV may be NULL) */
+    int blocks_per_sm; /* launch shape of the persistent kernels (4 warps per block); 0 = library default */
+    int varsize_order; /* mixed-size batches: 0 (default) largest order first, 1 smallest first */
+    int shift_sweeps;  /* ves_eigensolve_shifts: sweeps per eigenvalue that use a predicted shift; default 1 */
+    int reserved[2];
 } ves_options;
 
 void ves_default_options(ves_options *opt);
@@ -150,6 +157,102 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt,
                    const double *rA, const double *iA, double *rE, double *iE, double *rV, double *iV,
                    double *rT, double *iT, int *status, int *sweeps,
                    const ves_options *opt, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Mixed-size batches (no counterpart in the reference, which solves one order
+ * per call).  `count` matrices, matrix m of order dims[m] (device array), in
+ * the packed layout: its dims[m]^2 elements column-major and contiguous at
+ * element offset sum_{j<m} dims[j]^2 of each plane (rA, iA; the same layout for
+ * rV, iV), its eigenvalues at sum_{j<m} dims[j] of rE, iE.  Orders must lie in
+ * [1, max_dim] with max_dim <= VES_VARSIZE_MAX_DIM; other matrices are skipped
+ * and flagged VES_STATUS_BAD_DIM.  The batch is binned by order on the device
+ * and solved by one persistent FP64 launch (largest orders first unless
+ * varsize_order = 1); no host synchronisation, so the call can be captured in
+ * a CUDA graph (see ves_graph_capture_varsize).  workspace must hold
+ * ves_eigensolve_varsize_workspace_size() bytes (or be NULL: cached). */
+#define VES_VARSIZE_MAX_DIM 64
+size_t ves_eigensolve_varsize_workspace_size(long long count, int max_dim, const ves_options *opt);
+int ves_eigensolve_varsize(long long count, int max_dim, const int *dims,
+                           const double *rA, const double *iA, double *rE, double *iE, double *rV, double *iV,
+                           int *status, int *sweeps, const ves_options *opt,
+                           void *workspace, size_t workspace_bytes, void *stream);
+
+/* A CUDA graph of one ves_eigensolve_varsize call (pointers, count and
+ * options are baked in; the contents of dims and A may change between
+ * launches).  workspace must not be NULL.  Replay with ves_graph_launch. */
+typedef struct ves_graph ves_graph;
+int ves_graph_capture_varsize(ves_graph **out, long long count, int max_dim, const int *dims,
+                              const double *rA, const double *iA, double *rE, double *iE, double *rV, double *iV,
+                              int *status, int *sweeps, const ves_options *opt,
+                              void *workspace, size_t workspace_bytes);
+int ves_graph_launch(ves_graph *graph, void *stream);
+void ves_graph_destroy(ves_graph *graph);
+
+/* ---- learned shifts (no counterpart in the reference) ------------------------
+ * ves_eigensolve_shifts: the FP64 solver of ves_eigensolve, except that for the
+ * first opt->shift_sweeps sweeps of each eigenvalue the QR shift is the unused
+ * predicted eigenvalue nearest to the Wilkinson estimate (rS, iS: n predictions
+ * per matrix, SoA vectors like rE, iE).  After those sweeps, at the exceptional
+ * sweeps, and whenever predictions run out, the reference's shifts are used;
+ * results carry the same backward-error guarantee.  fallbacks (nullable) gets
+ * per matrix the number of eigenvalues that needed more than shift_sweeps + 2
+ * sweeps (VES_STATUS_SHIFT_FALLBACK marks those matrices). */
+int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt,
+                          const double *rA, const double *iA, double *rE, double *iE, double *rV, double *iV,
+                          const double *rS, const double *iS, int *status, int *sweeps, int *fallbacks,
+                          const ves_options *opt, void *workspace, size_t workspace_bytes, void *stream);
+
+/* The shift network: features [family parameters (n_params per matrix, a
+ * row-major FP64 device array), Re diag A, Im diag A] -> n predicted
+ * eigenvalues; hidden layers of `hidden` units (multiple of 16, <= 256), GELU,
+ * BF16 on the tcgen05 tensor cores.  Trained on eigenvalues from the FP64
+ * solver (rE, iE in the SoA layout of rA, iA).  Checkpoints are flat binary. */
+typedef struct ves_shiftnet ves_shiftnet;
+int ves_shiftnet_create(ves_shiftnet **net, int dim, int n_params, int hidden, unsigned long long seed);
+void ves_shiftnet_destroy(ves_shiftnet *net);
+int ves_shiftnet_train(ves_shiftnet *net, long long count, int thread_cnt, const double *params,
+                       const double *rA, const double *iA, const double *rE, const double *iE,
+                       int epochs, int batch, float lr, unsigned long long seed, float *loss_per_epoch, void *stream);
+size_t ves_shiftnet_predict_workspace_size(const ves_shiftnet *net, long long count);
+int ves_shiftnet_predict(const ves_shiftnet *net, long long count, int thread_cnt, const double *params,
+                         const double *rA, const double *iA, double *rS, double *iS,
+                         void *workspace, size_t workspace_bytes, void *stream);
+int ves_shiftnet_save(const ves_shiftnet *net, const char *path);
+int ves_shiftnet_load(ves_shiftnet **net, const char *path);
+
+/* The learned-shift network's GEMM on the tcgen05 tensor cores: C = A * B
+ * (+ bias) (GELU if act = 1), A row-major M x K BF16 (lda), Bt = B transposed,
+ * row-major N x K BF16 (ldb); C (nullable) gets act(A*B + bias) as BF16 and Cf
+ * (nullable) the pre-activation A*B + bias as FP32, both row-major M x N with
+ * leading dimension ldc; K, lda, ldb multiples of 8 and
+ * 16-byte aligned rows.  `err` (device int, nullable) is set to 1 if the
+ * tensor-core pipeline did not complete.  No counterpart in the reference. */
+int ves_gemm_bf16(int M, int N, int K, const void *A, int lda, const void *Bt, int ldb, const float *bias, int act,
+                  void *C, float *Cf, int ldc, int *err, void *stream);
+
+/* Roots of polynomials c_0 + c_1 x + ... + c_d x^d (d = degree), as eigenvalues
+ * of their companion matrices (the reference's create_companion_matrices +
+ * zlahqr kernel, Toolbox.hpp:607-643, :1894-1957), on the eigenvalues-only QR.
+ * Coefficients: SoA vectors of length degree+1 per polynomial (rC, iC: element i
+ * of polynomial m = b*thread_cnt + t at b*thread_cnt*(degree+1) + i*thread_cnt + t);
+ * roots: SoA vectors of length degree.  A zero leading coefficient or non-finite
+ * data gives NaN roots and VES_STATUS_NONFINITE.  workspace as ves_eigensolve. */
+size_t ves_polyroots_workspace_size(int degree, int block_cnt, int thread_cnt);
+int ves_polyroots(int degree, int block_cnt, int thread_cnt, const double *rC, const double *iC,
+                  double *rR, double *iR, int *status, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Device transposes between the SoA planes and interleaved complex batches
+ * (re, im pairs; matrix m at z + 2*m*dim*dim, row-major i.e. C/NumPy order if
+ * row_major != 0, else column-major), and the same for length-dim vectors.
+ * z must be 16-byte aligned.  Replace the host-side rearrangeMatrices /
+ * arrangeMatricesAoS (utils.cpp:85-123) for interleaved complex data. */
+int ves_soa_from_complex(int dim, int block_cnt, int thread_cnt, const void *z, int row_major,
+                         double *re, double *im, void *stream);
+int ves_complex_from_soa(int dim, int block_cnt, int thread_cnt, const double *re, const double *im,
+                         int row_major, void *z, void *stream);
+int ves_soa_vec_from_complex(int dim, int block_cnt, int thread_cnt, const void *z, double *re, double *im,
+                             void *stream);
+int ves_complex_from_soa_vec(int dim, int block_cnt, int thread_cnt, const double *re, const double *im,
+                             void *z, void *stream);
 
 /* Stage entry points on device data (same semantics as the drop-ins above). */
 int ves_zgehrd(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau, void *stream);

@@ -1,0 +1,82 @@
+"""Learned shifts: whatever the predictions, the solve meets the same bar as
+the plain FP64 solver (the reference's shifts take over after the first
+sweep); good predictions cut the sweep count; the network trains, predicts,
+and round-trips through its checkpoint."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+import learned_shift
+import ves
+from gpu_util import soa_planes_to_batch, soa_vec_to_batch, device_residuals
+from parity import match_eigs
+
+pytestmark = pytest.mark.gpu
+TC = 512
+
+
+def solve_shifts(n, N, rA, iA, rS, iS, **opt):
+    import torch
+    rE = torch.empty(N * n, dtype=torch.float64, device="cuda")
+    iE = torch.empty_like(rE)
+    rV, iV = torch.empty_like(rA), torch.empty_like(iA)
+    st = torch.zeros(N, dtype=torch.int32, device="cuda")
+    sw = torch.zeros(N, dtype=torch.int32, device="cuda")
+    fb = torch.zeros(N, dtype=torch.int32, device="cuda")
+    ves.eigensolve_shifts(n, N // TC, TC, rA, iA, rE, iE, rV, iV, rS, iS, status=st, sweeps=sw, fallbacks=fb,
+                          options=ves.default_options(**opt))
+    torch.cuda.synchronize()
+    res = device_residuals(soa_planes_to_batch(rA, iA, n, TC), soa_vec_to_batch(rE, iE, n, TC),
+                           soa_planes_to_batch(rV, iV, n, TC))
+    return rE, iE, st, sw, fb, float(res.max())
+
+
+@pytest.mark.parametrize("n", [8, 16, 24])
+def test_exact_and_garbage_predictions(n):
+    import torch
+    N = 4096
+    p, rA, iA = learned_shift.family(N, n, param_seed=11)
+    rE0, iE0, sw0 = learned_shift.solve_plain(n, N, rA, iA, TC)
+    E0 = ves.complex_vec_from_soa(rE0.cpu().numpy(), iE0.cpu().numpy(), n, TC)
+    nA = np.linalg.norm(ves.complex_from_soa(rA.cpu().numpy(), iA.cpu().numpy(), n, TC), axis=(1, 2))
+    # exact eigenvalues as predictions: same spectrum, fewer sweeps
+    rE, iE, st, sw, fb, res = solve_shifts(n, N, rA, iA, rE0, iE0)
+    assert res <= 1e-13
+    _, err, _ = match_eigs(ves.complex_vec_from_soa(rE.cpu().numpy(), iE.cpu().numpy(), n, TC), E0)
+    assert (err / nA).max() <= 1e-12
+    assert sw.double().mean().item() < 0.8 * sw0.double().mean().item()
+    # useless predictions (all far away): still correct, fallbacks reported
+    far = torch.full_like(rE0, 100.0)
+    rE, iE, st, sw, fb, res = solve_shifts(n, N, rA, iA, far, torch.zeros_like(far))
+    assert res <= 1e-13
+    _, err, _ = match_eigs(ves.complex_vec_from_soa(rE.cpu().numpy(), iE.cpu().numpy(), n, TC), E0)
+    assert (err / nA).max() <= 1e-12
+    assert fb.sum().item() > 0 and ((st & ves.VES_STATUS_SHIFT_FALLBACK) != 0).any()
+
+
+def test_train_predict_checkpoint():
+    import torch
+    n, N = 8, 16384
+    net, losses = learned_shift.train(n, count=N, epochs=8, batch=512, lr=2e-3, hidden=128, param_seed=21)
+    assert np.isfinite(losses).all()
+    assert losses[-1] < 0.5 * losses[0]
+    p, rA, iA = learned_shift.family(4096, n, param_seed=22)
+    rE, iE, _ = learned_shift.solve_plain(n, 4096, rA, iA, TC)
+    rS, iS = learned_shift.predict(net, n, 4096, p, rA, iA)
+    torch.cuda.synchronize()
+    err_net = learned_shift.prediction_error(n, 4096, rS, iS, rE, iE)
+    # the diagonal of A(p) is the trivial guess the network must beat
+    A = ves.complex_from_soa(rA.cpu().numpy(), iA.cpu().numpy(), n, TC)
+    E = ves.complex_vec_from_soa(rE.cpu().numpy(), iE.cpu().numpy(), n, TC)
+    d = np.diagonal(A, axis1=1, axis2=2)
+    err_diag = np.abs(d[:, :, None] - E[:, None, :]).min(axis=2)
+    assert np.median(err_net) < 0.5 * np.median(err_diag)
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "net.bin")
+        net.save(path)
+        net2 = ves.ShiftNet(path=path)
+        rS2, iS2 = learned_shift.predict(net2, n, 4096, p, rA, iA)
+        torch.cuda.synchronize()
+        assert torch.equal(rS, rS2) and torch.equal(iS, iS2)

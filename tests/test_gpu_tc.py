@@ -1,0 +1,26 @@
+"""The learned-shift network's BF16 GEMM on the tcgen05 tensor cores against a
+plain fp32 product of the same BF16 values."""
+import pytest
+
+import ves
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (300, 256, 64), (1024, 256, 256), (77, 48, 256), (512, 64, 96),
+                                   (5, 16, 32)])
+@pytest.mark.parametrize("act", [0, 1])
+def test_gemm_bf16_matches_fp32_reference(M, N, K, act):
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(M * 7 + N + K)
+    A = torch.randn(M, K, generator=g, device="cuda").to(torch.bfloat16)
+    Bt = (torch.randn(N, K, generator=g, device="cuda") / K ** 0.5).to(torch.bfloat16)
+    bias = torch.randn(N, generator=g, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    C, Cf = ves.gemm_bf16(A, Bt, bias=bias, act=act, out_bf16=True, out_f32=True, err=err)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    z = A.float() @ Bt.float().T + bias  # Cf: pre-activation
+    ref = torch.nn.functional.gelu(z, approximate="tanh") if act else z
+    assert (Cf - z).abs().max().item() <= 1e-4 * (z.abs().max().item() + 1.0)
+    assert (C.float() - ref).abs().max().item() <= 1e-2 * (ref.abs().max().item() + 1.0)

@@ -132,9 +132,14 @@ struct WsPlan {
     size_t fp64, mixed, list, count, total;
 };
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
-WsPlan workspace_plan(int precision, int n, long long N)
+WsPlan workspace_plan(int precision, int n, long long N, bool vectors = true)
 {
     WsPlan p{};
+    if (!vectors) {
+        p.fp64 = align256(ves::eigvals_workspace_bytes(n, N));
+        p.total = p.fp64;
+        return p;
+    }
     p.fp64 = align256(ves::fused_workspace_bytes(n, N, nullptr, nullptr));
     if (precision == VES_PREC_FP32_REFINE) {
         p.mixed = align256(ves::mixed_workspace_bytes(n, N, nullptr, nullptr));
@@ -411,6 +416,10 @@ void ves_default_options(ves_options *opt)
     opt->vnorm = VES_VNORM_REFERENCE;
     opt->refine_steps = 3;
     opt->refine_tol = 5e-14;
+    opt->want_vectors = 1;
+    opt->blocks_per_sm = 0;
+    opt->varsize_order = 0;
+    opt->shift_sweeps = 1;
 }
 
 size_t ves_eigensolve_workspace_size(int dim, int block_cnt, int thread_cnt, const ves_options *opt)
@@ -420,7 +429,7 @@ size_t ves_eigensolve_workspace_size(int dim, int block_cnt, int thread_cnt, con
     ves_options o;
     ves_default_options(&o);
     if (opt) o = *opt;
-    return workspace_plan(o.precision, dim, g.N).total;
+    return workspace_plan(o.precision, dim, g.N, o.want_vectors != 0).total;
 }
 
 int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, const double *iA, double *rE, double *iE,
@@ -431,10 +440,18 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
     ves::Geom g;
     if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
     if (g.N == 0) return VES_OK;
-    if (!rA || !iA || !rE || !iE || !rV || !iV || (!rT) != (!iT)) { set_error("null pointer"); return VES_ERR_ARG; }
     ves_options o;
     ves_default_options(&o);
     if (opt) o = *opt;
+    const bool vectors = o.want_vectors != 0;
+    if (!rA || !iA || !rE || !iE || (vectors && (!rV || !iV)) || (!rT) != (!iT)) {
+        set_error("null pointer");
+        return VES_ERR_ARG;
+    }
+    if (!vectors && (rT || o.precision != VES_PREC_FP64)) {
+        set_error("eigenvalues only (want_vectors = 0) runs in FP64 and returns no Schur form");
+        return VES_ERR_UNSUPPORTED;
+    }
     if (o.precision != VES_PREC_FP64 && o.precision != VES_PREC_FP32_REFINE) {
         set_error("precision mode %d unknown", o.precision);
         return VES_ERR_ARG;
@@ -443,13 +460,17 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
         set_error("the Schur form output needs precision VES_PREC_FP64");
         return VES_ERR_UNSUPPORTED;
     }
+    if (o.precision == VES_PREC_FP32_REFINE && dim > 64) {
+        set_error("precision VES_PREC_FP32_REFINE supports dim <= 64 (dim=%d)", dim);
+        return VES_ERR_UNSUPPORTED;
+    }
     if (o.max_its < 0 || o.max_its > 10000) { set_error("max_its=%d outside [0, 10000]", o.max_its); return VES_ERR_ARG; }
     if (o.vnorm < 0 || o.vnorm > 2) { set_error("vnorm=%d unknown", o.vnorm); return VES_ERR_ARG; }
     if (o.refine_steps < 0 || o.refine_steps > 100 || !(o.refine_tol > 0.0)) {
         set_error("refine_steps=%d / refine_tol=%g out of range", o.refine_steps, o.refine_tol);
         return VES_ERR_ARG;
     }
-    const WsPlan plan = workspace_plan(o.precision, dim, g.N);
+    const WsPlan plan = workspace_plan(o.precision, dim, g.N, vectors);
     const size_t need = plan.total;
     void *ws = workspace;
     std::unique_lock<std::mutex> lk;
@@ -472,6 +493,9 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
     a.max_its = o.max_its;
     a.vnorm = o.vnorm;
     cudaStream_t st = (cudaStream_t)stream;
+    if (!vectors)
+        return native(cuda_ok(ves::launch_eigvals(g, rA, iA, rE, iE, status, sweeps, ws, o.max_its, st),
+                              "eigenvalues kernel launch"));
     if (o.precision == VES_PREC_FP64)
         return native(cuda_ok(ves::launch_fused_fp64(a, st), "eigensolve kernel launch"));
 
@@ -496,6 +520,264 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
     a.list = list;
     a.list_count = count;
     return native(cuda_ok(ves::launch_fused_fp64(a, st), "fallback kernel launch"));
+}
+
+size_t ves_polyroots_workspace_size(int degree, int block_cnt, int thread_cnt)
+{
+    ves::Geom g;
+    if (!geom_ok(degree, block_cnt, thread_cnt, &g)) return 0;
+    return align256(ves::eigvals_workspace_bytes(degree, g.N));
+}
+
+int ves_polyroots(int degree, int block_cnt, int thread_cnt, const double *rC, const double *iC, double *rR,
+                  double *iR, int *status, void *workspace, size_t workspace_bytes, void *stream)
+{
+    t_last_error.clear();
+    ves::Geom g;
+    if (!geom_ok(degree, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
+    if (g.N == 0) return VES_OK;
+    if (!rC || !iC || !rR || !iR) { set_error("null pointer"); return VES_ERR_ARG; }
+    const size_t need = align256(ves::eigvals_workspace_bytes(degree, g.N));
+    void *ws = workspace;
+    std::unique_lock<std::mutex> lk;
+    if (!ws) {
+        lk = std::unique_lock<std::mutex>(pool().mu);
+        ws = pool().get(14, need);
+        if (!ws) { set_error("device allocation of %zu workspace bytes failed", need); return VES_ERR_NOMEM; }
+    } else if (workspace_bytes < need || ((uintptr_t)ws & 255)) {
+        set_error("workspace: %zu bytes given, %zu needed (256-byte aligned)", workspace_bytes, need);
+        return VES_ERR_ARG;
+    }
+    return native(cuda_ok(ves::launch_polyroots(g, rC, iC, rR, iR, status, ws, 30, (cudaStream_t)stream),
+                          "polyroots kernel launch"));
+}
+
+static int transpose_call(bool to_soa, bool vec, int dim, int block_cnt, int thread_cnt, const double *re_in,
+                          const double *im_in, double *re_out, double *im_out, const void *z_in, void *z_out,
+                          int row_major, void *stream)
+{
+    t_last_error.clear();
+    ves::Geom g;
+    if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
+    if (g.N == 0) return VES_OK;
+    const void *zp = to_soa ? z_in : z_out;
+    if (!zp || (to_soa ? (!re_out || !im_out) : (!re_in || !im_in))) { set_error("null pointer"); return VES_ERR_ARG; }
+    if ((uintptr_t)zp & 15) { set_error("the interleaved complex array must be 16-byte aligned"); return VES_ERR_ARG; }
+    const long long len = vec ? dim : (long long)dim * dim;
+    return native(cuda_ok(ves::launch_transpose(to_soa, re_in, im_in, re_out, im_out, static_cast<const double *>(z_in),
+                                                static_cast<double *>(z_out), g.N, dim, len, thread_cnt,
+                                                !vec && row_major != 0, (cudaStream_t)stream),
+                          "transpose launch"));
+}
+
+int ves_soa_from_complex(int dim, int block_cnt, int thread_cnt, const void *z, int row_major, double *re, double *im,
+                         void *stream)
+{
+    return transpose_call(true, false, dim, block_cnt, thread_cnt, nullptr, nullptr, re, im, z, nullptr, row_major,
+                          stream);
+}
+
+int ves_complex_from_soa(int dim, int block_cnt, int thread_cnt, const double *re, const double *im, int row_major,
+                         void *z, void *stream)
+{
+    return transpose_call(false, false, dim, block_cnt, thread_cnt, re, im, nullptr, nullptr, nullptr, z, row_major,
+                          stream);
+}
+
+int ves_soa_vec_from_complex(int dim, int block_cnt, int thread_cnt, const void *z, double *re, double *im,
+                             void *stream)
+{
+    return transpose_call(true, true, dim, block_cnt, thread_cnt, nullptr, nullptr, re, im, z, nullptr, 0, stream);
+}
+
+int ves_complex_from_soa_vec(int dim, int block_cnt, int thread_cnt, const double *re, const double *im, void *z,
+                             void *stream)
+{
+    return transpose_call(false, true, dim, block_cnt, thread_cnt, re, im, nullptr, nullptr, nullptr, z, 0, stream);
+}
+
+int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *rA, const double *iA, double *rE,
+                          double *iE, double *rV, double *iV, const double *rS, const double *iS, int *status,
+                          int *sweeps, int *fallbacks, const ves_options *opt, void *workspace,
+                          size_t workspace_bytes, void *stream)
+{
+    t_last_error.clear();
+    ves::Geom g;
+    if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
+    if (dim > 64) { set_error("learned shifts support dim <= 64"); return VES_ERR_UNSUPPORTED; }
+    if (g.N == 0) return VES_OK;
+    if (!rA || !iA || !rE || !iE || !rV || !iV || !rS || !iS) { set_error("null pointer"); return VES_ERR_ARG; }
+    ves_options o;
+    ves_default_options(&o);
+    if (opt) o = *opt;
+    if (o.max_its < 0 || o.max_its > 10000 || o.vnorm < 0 || o.vnorm > 2 || o.shift_sweeps < 0 ||
+        o.shift_sweeps > 9) {
+        set_error("option out of range");
+        return VES_ERR_ARG;
+    }
+    const size_t need = align256(ves::fused_workspace_bytes(dim, g.N, nullptr, nullptr));
+    void *ws = workspace;
+    std::unique_lock<std::mutex> lk;
+    if (!ws) {
+        lk = std::unique_lock<std::mutex>(pool().mu);
+        ws = pool().get(12, need);
+        if (!ws) { set_error("device allocation of %zu workspace bytes failed", need); return VES_ERR_NOMEM; }
+    } else if (workspace_bytes < need || ((uintptr_t)ws & 255)) {
+        set_error("workspace: %zu bytes given, %zu needed (256-byte aligned)", workspace_bytes, need);
+        return VES_ERR_ARG;
+    }
+    ves::FusedArgs a{};
+    a.g = g;
+    a.rA = rA; a.iA = iA; a.rE = rE; a.iE = iE; a.rV = rV; a.iV = iV;
+    a.status = status; a.sweeps = sweeps;
+    a.ws = ws;
+    a.max_its = o.max_its;
+    a.vnorm = o.vnorm;
+    a.rS = rS; a.iS = iS;
+    a.shift_sweeps = o.shift_sweeps;
+    a.fallbacks = fallbacks;
+    return native(cuda_ok(ves::launch_fused_fp64(a, (cudaStream_t)stream), "learned-shift solve launch"));
+}
+
+int ves_gemm_bf16(int M, int N, int K, const void *A, int lda, const void *Bt, int ldb, const float *bias, int act,
+                  void *C, float *Cf, int ldc, int *err, void *stream)
+{
+    t_last_error.clear();
+    if (M < 0 || N < 0 || K < 0 || (K & 7) || (lda & 7) || (ldb & 7) || lda < K || ldb < K || ldc < N ||
+        act < 0 || act > 1) {
+        set_error("gemm: bad sizes (K, lda, ldb must be multiples of 8, lda, ldb >= K, ldc >= N)");
+        return VES_ERR_ARG;
+    }
+    if ((M && K && !A) || (N && K && !Bt) || (!C && !Cf) || ((uintptr_t)A & 15) || ((uintptr_t)Bt & 15)) {
+        set_error("gemm: null or misaligned pointer");
+        return VES_ERR_ARG;
+    }
+    return native(cuda_ok(ves::launch_gemm_bf16(M, N, K, A, lda, Bt, ldb, bias, act, C, Cf, ldc, err,
+                                                (cudaStream_t)stream),
+                          "gemm launch"));
+}
+
+static int varsize_bps(const ves_options &o) { return o.blocks_per_sm > 0 ? o.blocks_per_sm : 2; }
+
+size_t ves_eigensolve_varsize_workspace_size(long long count, int max_dim, const ves_options *opt)
+{
+    ves_options o;
+    ves_default_options(&o);
+    if (opt) o = *opt;
+    if (count < 0 || max_dim < 1 || max_dim > VES_VARSIZE_MAX_DIM) return 0;
+    return align256(ves::varsize_workspace_bytes(count, max_dim, varsize_bps(o)));
+}
+
+static int varsize_check(long long count, int max_dim, const int *dims, const double *rA, const double *iA,
+                         const double *rE, const double *iE, const double *rV, const double *iV,
+                         const ves_options &o)
+{
+    if (count < 0 || count > (1LL << 31) - 1) { set_error("count=%lld out of range", count); return VES_ERR_ARG; }
+    if (max_dim < 1 || max_dim > VES_VARSIZE_MAX_DIM) {
+        set_error("max_dim=%d outside [1, VES_VARSIZE_MAX_DIM=%d]", max_dim, VES_VARSIZE_MAX_DIM);
+        return VES_ERR_ARG;
+    }
+    if (count > 0 && (!dims || !rA || !iA || !rE || !iE || !rV || !iV)) { set_error("null pointer"); return VES_ERR_ARG; }
+    if (o.precision != VES_PREC_FP64 || !o.want_vectors) {
+        set_error("mixed-size batches run the FP64 eigenvalue-and-vector path");
+        return VES_ERR_UNSUPPORTED;
+    }
+    if (o.max_its < 0 || o.max_its > 10000 || o.vnorm < 0 || o.vnorm > 2 || o.blocks_per_sm < 0 ||
+        o.blocks_per_sm > 16 || o.varsize_order < 0 || o.varsize_order > 1) {
+        set_error("option out of range");
+        return VES_ERR_ARG;
+    }
+    return VES_OK;
+}
+
+int ves_eigensolve_varsize(long long count, int max_dim, const int *dims, const double *rA, const double *iA,
+                           double *rE, double *iE, double *rV, double *iV, int *status, int *sweeps,
+                           const ves_options *opt, void *workspace, size_t workspace_bytes, void *stream)
+{
+    t_last_error.clear();
+    ves_options o;
+    ves_default_options(&o);
+    if (opt) o = *opt;
+    int rc = varsize_check(count, max_dim, dims, rA, iA, rE, iE, rV, iV, o);
+    if (rc != VES_OK || count == 0) return rc;
+    const size_t need = align256(ves::varsize_workspace_bytes(count, max_dim, varsize_bps(o)));
+    void *ws = workspace;
+    std::unique_lock<std::mutex> lk;
+    if (!ws) {
+        lk = std::unique_lock<std::mutex>(pool().mu);
+        ws = pool().get(13, need);
+        if (!ws) { set_error("device allocation of %zu workspace bytes failed", need); return VES_ERR_NOMEM; }
+    } else if (workspace_bytes < need || ((uintptr_t)ws & 255)) {
+        set_error("workspace: %zu bytes given, %zu needed (256-byte aligned)", workspace_bytes, need);
+        return VES_ERR_ARG;
+    }
+    return native(cuda_ok(ves::launch_varsize(count, max_dim, dims, rA, iA, rE, iE, rV, iV, status, sweeps, ws,
+                                              o.max_its, o.vnorm, varsize_bps(o), o.varsize_order,
+                                              (cudaStream_t)stream),
+                          "mixed-size solve launch"));
+}
+
+}  // extern "C"
+
+struct ves_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" {
+
+int ves_graph_capture_varsize(ves_graph **out, long long count, int max_dim, const int *dims, const double *rA,
+                              const double *iA, double *rE, double *iE, double *rV, double *iV, int *status,
+                              int *sweeps, const ves_options *opt, void *workspace, size_t workspace_bytes)
+{
+    t_last_error.clear();
+    if (!out) { set_error("null pointer"); return VES_ERR_ARG; }
+    *out = nullptr;
+    ves_options o;
+    ves_default_options(&o);
+    if (opt) o = *opt;
+    int rc = varsize_check(count, max_dim, dims, rA, iA, rE, iE, rV, iV, o);
+    if (rc != VES_OK) return rc;
+    const size_t need = align256(ves::varsize_workspace_bytes(count, max_dim, varsize_bps(o)));
+    if (!workspace || workspace_bytes < need || ((uintptr_t)workspace & 255)) {
+        set_error("graph capture needs a caller workspace of %zu bytes (256-byte aligned)", need);
+        return VES_ERR_ARG;
+    }
+    cudaStream_t cs = nullptr;
+    if (!cuda_ok(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream")) return VES_ERR_CUDA;
+    ves_graph *g = new ves_graph();
+    bool ok = cuda_ok(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (ok) {
+        const cudaError_t le = ves::launch_varsize(count, max_dim, dims, rA, iA, rE, iE, rV, iV, status, sweeps,
+                                                   workspace, o.max_its, o.vnorm, varsize_bps(o), o.varsize_order, cs);
+        const cudaError_t ee = cudaStreamEndCapture(cs, &g->graph);
+        ok = cuda_ok(le, "captured launch") && cuda_ok(ee, "end capture");
+    }
+    if (ok) ok = cuda_ok(cudaGraphInstantiate(&g->exec, g->graph, 0), "graph instantiate");
+    cudaStreamDestroy(cs);
+    if (!ok) {
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+        if (g->graph) cudaGraphDestroy(g->graph);
+        delete g;
+        return VES_ERR_CUDA;
+    }
+    *out = g;
+    return VES_OK;
+}
+
+int ves_graph_launch(ves_graph *graph, void *stream)
+{
+    t_last_error.clear();
+    if (!graph || !graph->exec) { set_error("null graph"); return VES_ERR_ARG; }
+    return native(cuda_ok(cudaGraphLaunch(graph->exec, (cudaStream_t)stream), "graph launch"));
+}
+
+void ves_graph_destroy(ves_graph *graph)
+{
+    if (!graph) return;
+    if (graph->exec) cudaGraphExecDestroy(graph->exec);
+    if (graph->graph) cudaGraphDestroy(graph->graph);
+    delete graph;
 }
 
 int ves_zgehrd(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau, void *stream)

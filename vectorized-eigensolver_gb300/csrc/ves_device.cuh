@@ -28,6 +28,7 @@ constexpr int ST_ITCAP = 1;      // some eigenvalue hit the sweep cap (reference
 constexpr int ST_NONFINITE = 2;  // input held Inf/NaN
 constexpr int ST_SHIFT_FALLBACK = 4;  // learned shift abandoned for Wilkinson at least once
 constexpr int ST_REFINE_FALLBACK = 8; // mixed precision: pair did not converge, solved again in FP64
+constexpr int ST_BAD_DIM = 16;        // mixed-size batch: order outside the supported range, not solved
 
 template <class R> struct cx { R r, i; };
 
@@ -300,7 +301,7 @@ __device__ void clear_below_subdiag_lane(const int n, const M &H)
 // K loop over the union of the lanes' windows with a warp-uniform K, so each
 // matrix element access is the same offset for all lanes.
 // ---------------------------------------------------------------------------
-template <class R, class MH, class MZ>
+template <class R, bool kSchur = true, class MH, class MZ>
 __device__ void make_subdiag_real_lane(const int n, const MH &H, const MZ &Z)
 {
     for (int i = 2; i <= n; ++i) {
@@ -312,7 +313,8 @@ __device__ void make_subdiag_real_lane(const int n, const MH &H, const MZ &Z)
             for (int j = i; j <= n; ++j) H.st(i, j, cmul(H.ld(i, j), sc));
             const int re = (i + 1) < n ? (i + 1) : n;
             for (int j = 1; j <= re; ++j) H.st(j, i, cmulc(H.ld(j, i), sc));
-            for (int j = 1; j <= n; ++j) Z.st(j, i, cmulc(Z.ld(j, i), sc));
+            if (kSchur)
+                for (int j = 1; j <= n; ++j) Z.st(j, i, cmulc(Z.ld(j, i), sc));
         }
     }
 }
@@ -400,13 +402,57 @@ __device__ __forceinline__ void zlarfg2(cx<R> &v0, cx<R> &v1, cx<R> &t1)
     v0 = mk(-beta, R(0));
 }
 
-template <class R, class MH, class MZ>
+//
+// kSchur = false is the eigenvalues-only form (LAPACK wantT = wantZ = false,
+// the reference's dead zlahqr_ at Toolbox.hpp:1663-1890): only the active block
+// L..I is transformed (I1 = L, I2 = I) and Z is never touched.  The arithmetic
+// on the active block is the same as with kSchur = true, so the eigenvalues
+// are the same bit for bit.
+// Shift providers for zlahqr_warp.  NoShiftPredictions: the reference's
+// Wilkinson / exceptional shifts only.  ShiftPredictions: n predicted
+// eigenvalues per matrix (the learned-shift network's output); for the first
+// `sweeps` sweeps of each eigenvalue the unused prediction nearest to the
+// Wilkinson estimate replaces it, after which (and for the exceptional shifts)
+// the reference's shifts take over.  An eigenvalue that still needs more than
+// sweeps + 2 sweeps counts as a fallback to Wilkinson.
+struct NoShiftPredictions {
+    template <class R> __device__ __forceinline__ void pick(int, int, cx<R> &) {}
+    __device__ __forceinline__ void deflated(int) {}
+};
+struct ShiftPredictions {
+    const double *re, *im;  // this matrix's predictions, stride s
+    long long s;
+    int n, sweeps;
+    unsigned long long used;
+    int current;
+    int fallbacks;
+    template <class R> __device__ __forceinline__ void pick(int its, int, cx<R> &t)
+    {
+        if (its >= sweeps || its == 10 || its == 20) return;
+        if (its == 0) {
+            R best = R(0);
+            int bi = -1;
+            for (int k = 0; k < n; ++k) {
+                if ((used >> k) & 1ULL) continue;
+                const R dr = (R)re[k * s] - t.r, di = (R)im[k * s] - t.i;
+                const R d = dr * dr + di * di;
+                if (bi < 0 || d < best) { best = d; bi = k; }
+            }
+            current = bi;
+            if (bi >= 0) used |= 1ULL << bi;
+        }
+        if (current >= 0) t = mk((R)re[current * s], (R)im[current * s]);
+    }
+    __device__ __forceinline__ void deflated(int its) { if (its > sweeps + 2) ++fallbacks; }
+};
+
+template <class R, bool kSchur = true, class MH, class MZ, class SP = NoShiftPredictions>
 __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool valid, const int max_its,
-                            int &nsweeps, int &status)
+                            int &nsweeps, int &status, SP *sp = nullptr)
 {
     const R ulp = lim<R>::eps();
     const R smlnum = lim<R>::tiny() * (R(n) / ulp);
-    if (valid) make_subdiag_real_lane<R>(n, H, Z);
+    if (valid) make_subdiag_real_lane<R, kSchur>(n, H, Z);
 
     // Lane state: active block L..I and the sweep count at this I.  As in the
     // reference, L only moves up while I stays, and resets to 1 when I moves.
@@ -421,8 +467,13 @@ __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool va
                 if (its > max_its) { status |= ST_ITCAP; --I; L = 1; its = 0; continue; }
                 L = deflation_scan<R>(I, L, H, n, ulp, smlnum);
                 if (L > 1) H.st(L, L - 1, mk(R(0), R(0)));
-                if (L >= I) { --I; L = 1; its = 0; continue; }
-                const cx<R> t = qr_shift<R>(I, L, its, H);
+                if (L >= I) {
+                    if (sp) sp->deflated(its);
+                    --I; L = 1; its = 0;
+                    continue;
+                }
+                cx<R> t = qr_shift<R>(I, L, its, H);
+                if (sp) sp->template pick<R>(its, I, t);
                 const cx<R> h11s = csub(H.ld(L, L), t);
                 const R h21 = H.ld(L + 1, L).r;
                 const R rs = R(1) / (cabs1(h11s) + fabs(h21));
@@ -448,27 +499,40 @@ __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool va
                 w1 = a1;
             }
             const R t2 = t1.r * w1.r - t1.i * w1.i;
-            if (act) {
-                // rows K, K+1, columns K..n (wantT: I2 = n)
+            if (kSchur) {
+                if (act) {
+                    // rows K, K+1, columns K..n (wantT: I2 = n)
+                    const cx<R> c1 = conj(t1);
+                    for (int j = K; j <= n; ++j) {
+                        cx<R> h1 = H.ld(K, j), h2 = H.ld(K + 1, j);
+                        rot_pair(h1, h2, c1, t2, w1);
+                        H.st(K, j, h1);
+                        H.st(K + 1, j, h2);
+                    }
+                }
+            } else {
+                // rows K, K+1, columns K..I (I2 = I, per lane)
                 const cx<R> c1 = conj(t1);
-                for (int j = K; j <= n; ++j) {
-                    cx<R> h1 = H.ld(K, j), h2 = H.ld(K + 1, j);
-                    rot_pair(h1, h2, c1, t2, w1);
-                    H.st(K, j, h1);
-                    H.st(K + 1, j, h2);
+                for (int j = K; j <= Kmax + 1; ++j) {
+                    if (act && j <= I) {
+                        cx<R> h1 = H.ld(K, j), h2 = H.ld(K + 1, j);
+                        rot_pair(h1, h2, c1, t2, w1);
+                        H.st(K, j, h1);
+                        H.st(K + 1, j, h2);
+                    }
                 }
             }
-            // columns K, K+1, rows 1..min(K+2, I)
+            // columns K, K+1, rows I1..min(K+2, I) (I1 = 1, or L without the Schur form)
             const int je = (K + 2) < n ? (K + 2) : n;
-            for (int j = 1; j <= je; ++j) {
-                if (act && j <= I) {
+            for (int j = kSchur ? 1 : Kmin; j <= je; ++j) {
+                if (act && j <= I && (kSchur || j >= L)) {
                     cx<R> h1 = H.ld(j, K), h2 = H.ld(j, K + 1);
                     rot_pair(h1, h2, t1, t2, conj(w1));
                     H.st(j, K, h1);
                     H.st(j, K + 1, h2);
                 }
             }
-            if (act) {
+            if (kSchur && act) {
                 const cx<R> cw = conj(w1);
                 for (int j = 1; j <= n; ++j) {
                     cx<R> z1 = Z.ld(j, K), z2 = Z.ld(j, K + 1);
@@ -485,9 +549,11 @@ __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool va
                 const R d = cabs(h);
                 const cx<R> z = conj(cscal(h, R(1) / d));
                 H.st(I, I - 1, mk(d, R(0)));
-                for (int j = I + 1; j <= n; ++j) H.st(I, j, cmul(H.ld(I, j), z));
-                for (int j = 1; j <= I - 1; ++j) H.st(j, I, cmulc(H.ld(j, I), z));
-                for (int j = 1; j <= n; ++j) Z.st(j, I, cmulc(Z.ld(j, I), z));
+                if (kSchur)
+                    for (int j = I + 1; j <= n; ++j) H.st(I, j, cmul(H.ld(I, j), z));
+                for (int j = kSchur ? 1 : L; j <= I - 1; ++j) H.st(j, I, cmulc(H.ld(j, I), z));
+                if (kSchur)
+                    for (int j = 1; j <= n; ++j) Z.st(j, I, cmulc(Z.ld(j, I), z));
             }
         }
     }

@@ -30,6 +30,12 @@ struct FusedArgs {
     // mixed-precision form's fallback pass); status gets ST_REFINE_FALLBACK
     const int *list;
     const int *list_count;
+    // optional predicted eigenvalues (SoA vectors, n per matrix) used as the
+    // first `shift_sweeps` QR shifts of every eigenvalue; `fallbacks` (nullable)
+    // counts per matrix the eigenvalues that still needed Wilkinson's shift
+    const double *rS, *iS;
+    int shift_sweeps;
+    int *fallbacks;
 };
 
 struct MixedArgs {
@@ -71,6 +77,28 @@ cudaError_t launch_backsubs(Geom g, const double *rT, const double *iT, double *
 // The FP64 fused kernel on a caller-chosen grid of `blocks` x 4 warps; the
 // workspace must hold blocks * 4 warp slots.
 cudaError_t launch_fused_fp64_blocks(const FusedArgs &a, int blocks, cudaStream_t st);
+
+// Eigenvalues only (no Q, no Schur vectors), companion-matrix roots, and the
+// SoA <-> interleaved-complex transposes.
+size_t eigvals_workspace_bytes(int n, long long N);
+cudaError_t launch_eigvals(Geom g, const double *rA, const double *iA, double *rE, double *iE, int *status,
+                           int *sweeps, void *ws, int max_its, cudaStream_t st);
+cudaError_t launch_polyroots(Geom g, const double *rC, const double *iC, double *rR, double *iR, int *status,
+                             void *ws, int max_its, cudaStream_t st);
+cudaError_t launch_transpose(bool to_soa, const double *src_re, const double *src_im, double *dst_re, double *dst_im,
+                             const double *z_in, double *z_out, long long N, int n, long long len, int tc,
+                             bool row_major, cudaStream_t st);
+
+// Mixed-size (packed) batches: binned by order, one persistent solve.
+size_t varsize_workspace_bytes(long long count, int max_dim, int blocks_per_sm);
+cudaError_t launch_varsize(long long count, int max_dim, const int *dims, const double *rA, const double *iA,
+                           double *rE, double *iE, double *rV, double *iV, int *status, int *sweeps, void *ws,
+                           int max_its, int vnorm, int blocks_per_sm, int order, cudaStream_t st);
+
+// BF16 GEMM on tcgen05 (C = A * B, Bt = B transposed, both K-major), bias and
+// GELU (act = 1) fused; C (BF16) and/or Cf (FP32) written.
+cudaError_t launch_gemm_bf16(int M, int N, int K, const void *A, int lda, const void *Bt, int ldb, const float *bias,
+                             int act, void *C, float *Cf, int ldc, int *err, cudaStream_t st);
 
 // Record the calling thread's message for ves_last_error().
 void set_error_message(const char *msg);

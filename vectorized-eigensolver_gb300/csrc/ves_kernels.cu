@@ -55,6 +55,7 @@ __device__ void write_vectors(const int n, const MZ &Z, const MatSoA<R> &V, cons
     }
 }
 
+template <bool kLearned>
 __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedArgs a)
 {
     const int n = a.g.n, tc = a.g.tc;
@@ -93,8 +94,23 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
             zunghr_lane<double>(n, H, Z, W);
             clear_below_subdiag_lane<double>(n, H);
         }
-        zlahqr_warp<double>(n, H, Z, valid && !(status & ST_NONFINITE), a.max_its, sweeps, status);
+        ShiftPredictions sp{};
+        if (kLearned) {
+            sp.re = a.rS + vo;
+            sp.im = a.iS + vo;
+            sp.s = tc;
+            sp.n = n;
+            sp.sweeps = a.shift_sweeps;
+            sp.used = 0;
+            sp.current = -1;
+            sp.fallbacks = 0;
+            zlahqr_warp<double, true>(n, H, Z, valid && !(status & ST_NONFINITE), a.max_its, sweeps, status, &sp);
+            if (sp.fallbacks) status |= ST_SHIFT_FALLBACK;
+        } else {
+            zlahqr_warp<double>(n, H, Z, valid && !(status & ST_NONFINITE), a.max_its, sweeps, status);
+        }
         if (valid) {
+            if (kLearned && a.fallbacks) a.fallbacks[m] = sp.fallbacks;
             const VecSoA<double> E{a.rE + vo, a.iE + vo, tc};
             for (int k = 1; k <= n; ++k) E.st(k, H.ld(k, k));
             if (a.rT) {
@@ -261,14 +277,17 @@ cudaError_t launch_fused_fp64(const FusedArgs &a, cudaStream_t st)
     if (a.g.N <= 0) return cudaSuccess;
     int blocks = 0, threads = 0;
     fused_workspace_bytes(a.g.n, a.g.N, &blocks, &threads);
-    fused_fp64_kernel<<<blocks, threads, 0, st>>>(a);
+    if (a.rS)
+        fused_fp64_kernel<true><<<blocks, threads, 0, st>>>(a);
+    else
+        fused_fp64_kernel<false><<<blocks, threads, 0, st>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_fused_fp64_blocks(const FusedArgs &a, int blocks, cudaStream_t st)
 {
     if (a.g.N <= 0) return cudaSuccess;
-    fused_fp64_kernel<<<blocks, kFusedThreads, 0, st>>>(a);
+    fused_fp64_kernel<false><<<blocks, kFusedThreads, 0, st>>>(a);
     return cudaGetLastError();
 }
 

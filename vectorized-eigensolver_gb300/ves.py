@@ -19,6 +19,7 @@ VES_STATUS_ITCAP = 1
 VES_STATUS_NONFINITE = 2
 VES_STATUS_SHIFT_FALLBACK = 4
 VES_STATUS_REFINE_FALLBACK = 8
+VES_STATUS_BAD_DIM = 16
 VES_PREC_FP64 = 0
 VES_PREC_FP32_REFINE = 1
 VNORM_REFERENCE, VNORM_MAX, VNORM_TWO = 0, 1, 2
@@ -35,7 +36,8 @@ class VesError(RuntimeError):
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", _int), ("max_its", _int), ("vnorm", _int), ("refine_steps", _int),
-                ("refine_tol", _dbl), ("reserved", _int * 6)]
+                ("refine_tol", _dbl), ("want_vectors", _int), ("blocks_per_sm", _int), ("varsize_order", _int),
+                ("shift_sweeps", _int), ("reserved", _int * 2)]
 
 
 # exported symbol -> (restype, argtypes); every name declared in include/ves.h
@@ -64,6 +66,30 @@ SIGNATURES = {
     "ves_zgemv": (_int, [_bool, _int, _int, _int, _VP, _VP, _VP, _VP, _VP, _VP, _dbl, _dbl, _VP]),
     "ves_backsubstitution": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP, _VP]),
     "ves_fp64_fma_rate": (_int, [_D, _VP]),
+    "ves_polyroots_workspace_size": (_size, [_int, _int, _int]),
+    "ves_eigensolve_varsize_workspace_size": (_size, [ctypes.c_longlong, _int, ctypes.POINTER(Options)]),
+    "ves_eigensolve_varsize": (_int, [ctypes.c_longlong, _int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
+                                      ctypes.POINTER(Options), _VP, _size, _VP]),
+    "ves_graph_capture_varsize": (_int, [ctypes.POINTER(_VP), ctypes.c_longlong, _int, _VP, _VP, _VP, _VP, _VP, _VP,
+                                         _VP, _VP, _VP, ctypes.POINTER(Options), _VP, _size]),
+    "ves_graph_launch": (_int, [_VP, _VP]),
+    "ves_eigensolve_shifts": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
+                                     ctypes.POINTER(Options), _VP, _size, _VP]),
+    "ves_shiftnet_create": (_int, [ctypes.POINTER(_VP), _int, _int, _int, ctypes.c_ulonglong]),
+    "ves_shiftnet_destroy": (None, [_VP]),
+    "ves_shiftnet_train": (_int, [_VP, ctypes.c_longlong, _int, _VP, _VP, _VP, _VP, _VP, _int, _int,
+                                  ctypes.c_float, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_float), _VP]),
+    "ves_shiftnet_predict_workspace_size": (_size, [_VP, ctypes.c_longlong]),
+    "ves_shiftnet_predict": (_int, [_VP, ctypes.c_longlong, _int, _VP, _VP, _VP, _VP, _VP, _VP, _size, _VP]),
+    "ves_shiftnet_save": (_int, [_VP, ctypes.c_char_p]),
+    "ves_shiftnet_load": (_int, [ctypes.POINTER(_VP), ctypes.c_char_p]),
+    "ves_gemm_bf16": (_int, [_int, _int, _int, _VP, _int, _VP, _int, _VP, _int, _VP, _VP, _int, _VP, _VP]),
+    "ves_graph_destroy": (None, [_VP]),
+    "ves_polyroots": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP, _VP, _VP, _size, _VP]),
+    "ves_soa_from_complex": (_int, [_int, _int, _int, _VP, _int, _VP, _VP, _VP]),
+    "ves_complex_from_soa": (_int, [_int, _int, _int, _VP, _VP, _int, _VP, _VP]),
+    "ves_soa_vec_from_complex": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP]),
+    "ves_complex_from_soa_vec": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP]),
     "ves_eigensolve_noalloc": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "ves_last_error": (ctypes.c_char_p, []),
     "ves_release": (None, []),
@@ -290,6 +316,142 @@ def eigensolve(dim, block_cnt, thread_cnt, rA, iA, rE, iE, rV, iV, rT=None, iT=N
                               _dp(rT), _dp(iT), _dp(status), _dp(sweeps), ctypes.byref(o), ws_ptr, ws_n,
                               _stream_ptr(stream))
     _check(rc, "ves_eigensolve")
+
+
+class DeviceBuffer:
+    """A 256-byte aligned device allocation (torch uint8 storage)."""
+
+    def __init__(self, nbytes, device=None):
+        import torch
+        self.nbytes = int(nbytes)
+        self.buf = torch.empty(max(self.nbytes, 1) + 256, dtype=torch.uint8, device=device or "cuda")
+        self.ptr = (self.buf.data_ptr() + 255) // 256 * 256
+
+
+def varsize_workspace(count, max_dim, options=None):
+    o = options if options is not None else default_options()
+    return DeviceBuffer(lib().ves_eigensolve_varsize_workspace_size(count, max_dim, ctypes.byref(o)))
+
+
+def eigensolve_varsize(count, max_dim, dims, rA, iA, rE, iE, rV, iV, status=None, sweeps=None, options=None,
+                       workspace=None, stream=None):
+    """ves_eigensolve_varsize on torch CUDA tensors (packed mixed-size layout)."""
+    o = options if options is not None else default_options()
+    ws_ptr, ws_n = (None, 0) if workspace is None else (ctypes.c_void_p(workspace.ptr), workspace.nbytes)
+    _check(lib().ves_eigensolve_varsize(count, max_dim, _dp(dims), _dp(rA), _dp(iA), _dp(rE), _dp(iE), _dp(rV),
+                                        _dp(iV), _dp(status), _dp(sweeps), ctypes.byref(o), ws_ptr, ws_n,
+                                        _stream_ptr(stream)), "ves_eigensolve_varsize")
+
+
+class VarsizeGraph:
+    """A captured CUDA graph of one mixed-size solve; replay with launch()."""
+
+    def __init__(self, count, max_dim, dims, rA, iA, rE, iE, rV, iV, status=None, sweeps=None, options=None,
+                 workspace=None):
+        o = options if options is not None else default_options()
+        self.workspace = workspace if workspace is not None else varsize_workspace(count, max_dim, o)
+        self.handle = _VP()
+        self._keep = (dims, rA, iA, rE, iE, rV, iV, status, sweeps)
+        _check(lib().ves_graph_capture_varsize(ctypes.byref(self.handle), count, max_dim, _dp(dims), _dp(rA),
+                                               _dp(iA), _dp(rE), _dp(iE), _dp(rV), _dp(iV), _dp(status),
+                                               _dp(sweeps), ctypes.byref(o), ctypes.c_void_p(self.workspace.ptr),
+                                               self.workspace.nbytes), "ves_graph_capture_varsize")
+
+    def launch(self, stream=None):
+        _check(lib().ves_graph_launch(self.handle, _stream_ptr(stream)), "ves_graph_launch")
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().ves_graph_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def eigensolve_shifts(dim, block_cnt, thread_cnt, rA, iA, rE, iE, rV, iV, rS, iS, status=None, sweeps=None,
+                      fallbacks=None, options=None, workspace=None, stream=None):
+    """ves_eigensolve_shifts on torch CUDA tensors (predicted shifts rS, iS)."""
+    o = options if options is not None else default_options()
+    ws_ptr, ws_n = (None, 0) if workspace is None else (ctypes.c_void_p(workspace.ptr), workspace.nbytes)
+    _check(lib().ves_eigensolve_shifts(dim, block_cnt, thread_cnt, _dp(rA), _dp(iA), _dp(rE), _dp(iE), _dp(rV),
+                                       _dp(iV), _dp(rS), _dp(iS), _dp(status), _dp(sweeps), _dp(fallbacks),
+                                       ctypes.byref(o), ws_ptr, ws_n, _stream_ptr(stream)), "ves_eigensolve_shifts")
+
+
+class ShiftNet:
+    """The learned-shift network (ves_shiftnet_*): features -> predicted eigenvalues."""
+
+    def __init__(self, dim=None, n_params=0, hidden=256, seed=0, path=None):
+        self.handle = _VP()
+        if path is not None:
+            _check(lib().ves_shiftnet_load(ctypes.byref(self.handle), path.encode()), "ves_shiftnet_load")
+        else:
+            _check(lib().ves_shiftnet_create(ctypes.byref(self.handle), dim, n_params, hidden, seed),
+                   "ves_shiftnet_create")
+
+    def train(self, count, thread_cnt, params, rA, iA, rE, iE, epochs=20, batch=1024, lr=1e-3, seed=0, stream=None):
+        losses = (ctypes.c_float * max(epochs, 1))()
+        _check(lib().ves_shiftnet_train(self.handle, count, thread_cnt, _dp(params), _dp(rA), _dp(iA), _dp(rE),
+                                        _dp(iE), epochs, batch, lr, seed, losses, _stream_ptr(stream)),
+               "ves_shiftnet_train")
+        return list(losses)[:epochs]
+
+    def predict(self, count, thread_cnt, params, rA, iA, rS, iS, stream=None):
+        ws = DeviceBuffer(lib().ves_shiftnet_predict_workspace_size(self.handle, count))
+        _check(lib().ves_shiftnet_predict(self.handle, count, thread_cnt, _dp(params), _dp(rA), _dp(iA), _dp(rS),
+                                          _dp(iS), ctypes.c_void_p(ws.ptr), ws.nbytes, _stream_ptr(stream)),
+               "ves_shiftnet_predict")
+        return ws
+
+    def save(self, path):
+        _check(lib().ves_shiftnet_save(self.handle, path.encode()), "ves_shiftnet_save")
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().ves_shiftnet_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def gemm_bf16(A, Bt, bias=None, act=0, out_bf16=True, out_f32=False, err=None, stream=None):
+    """C = A @ Bt.T (+ bias, GELU) on the tcgen05 tensor cores; A (M, K) and Bt (N, K)
+    contiguous bfloat16 CUDA tensors.  Returns (C_bf16 or None, C_f32 or None)."""
+    import torch
+    M, K = A.shape
+    N = Bt.shape[0]
+    C = torch.empty(M, N, dtype=torch.bfloat16, device=A.device) if out_bf16 else None
+    Cf = torch.empty(M, N, dtype=torch.float32, device=A.device) if out_f32 else None
+    _check(lib().ves_gemm_bf16(M, N, K, _dp(A), A.stride(0), _dp(Bt), Bt.stride(0), _dp(bias), act, _dp(C), _dp(Cf),
+                               N, _dp(err), _stream_ptr(stream)), "ves_gemm_bf16")
+    return C, Cf
+
+
+def polyroots(degree, block_cnt, thread_cnt, rC, iC, rR, iR, status=None, stream=None):
+    """Roots of SoA-stored polynomials (device tensors), see ves_polyroots."""
+    _check(lib().ves_polyroots(degree, block_cnt, thread_cnt, _dp(rC), _dp(iC), _dp(rR), _dp(iR), _dp(status), None, 0,
+                               _stream_ptr(stream)), "ves_polyroots")
+
+
+def soa_from_complex_dev(dim, block_cnt, thread_cnt, z, re, im, row_major=True, stream=None):
+    """Device: interleaved complex batch z (e.g. torch complex128 (N, n, n)) -> SoA planes."""
+    _check(lib().ves_soa_from_complex(dim, block_cnt, thread_cnt, _dp(z), int(row_major), _dp(re), _dp(im),
+                                      _stream_ptr(stream)), "ves_soa_from_complex")
+
+
+def complex_from_soa_dev(dim, block_cnt, thread_cnt, re, im, z, row_major=True, stream=None):
+    _check(lib().ves_complex_from_soa(dim, block_cnt, thread_cnt, _dp(re), _dp(im), int(row_major), _dp(z),
+                                      _stream_ptr(stream)), "ves_complex_from_soa")
+
+
+def soa_vec_from_complex_dev(dim, block_cnt, thread_cnt, z, re, im, stream=None):
+    _check(lib().ves_soa_vec_from_complex(dim, block_cnt, thread_cnt, _dp(z), _dp(re), _dp(im), _stream_ptr(stream)),
+           "ves_soa_vec_from_complex")
+
+
+def complex_from_soa_vec_dev(dim, block_cnt, thread_cnt, re, im, z, stream=None):
+    _check(lib().ves_complex_from_soa_vec(dim, block_cnt, thread_cnt, _dp(re), _dp(im), _dp(z), _stream_ptr(stream)),
+           "ves_complex_from_soa_vec")
 
 
 def zgehrd_dev(dim, block_cnt, thread_cnt, rA, iA, rtau, itau, stream=None):

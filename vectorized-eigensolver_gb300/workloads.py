@@ -58,3 +58,87 @@ def gaussian_soa(N, n, seed, thread_cnt):
         planes.append(np.ascontiguousarray(X.reshape(bc, thread_cnt, n, n).transpose(0, 3, 2, 1)).reshape(-1))
         del X
     return planes[0], planes[1]
+
+
+def _haar(gen, k, n, device):
+    import torch
+    G = torch.complex(torch.randn(k, n, n, generator=gen, dtype=torch.float64, device=device),
+                      torch.randn(k, n, n, generator=gen, dtype=torch.float64, device=device))
+    Q, R = torch.linalg.qr(G)
+    d = torch.diagonal(R, dim1=1, dim2=2)
+    return Q * (d / d.abs().clamp_min(1e-300))[:, None, :]  # Haar-distributed unitary
+
+
+def mixed_families(N, seed=2, nmin=4, nmax=64, device="cpu", as_list=True):
+    """The mixed-size workload: N complex128 matrices, order uniform in
+    [nmin, nmax], matrix m of family m % 3:
+      0  i.i.d. complex Gaussian;
+      1  non-normal A = V diag(l) V^-1, V = U diag(logspace(0, -4, n)) W with U, W
+         Haar unitary (cond(V) = 1e4), l uniform in the unit disk;
+      2  clustered A = X diag(l) X^-1, l = one of 4 complex-Gaussian centres plus
+         an offset uniform in a disk of radius 1e-6, X = U + 0.3 G (U Haar).
+    Generated with torch (seeded), batched by order.  Returns a list of (n, n)
+    numpy arrays (as_list) or (sizes, dict n -> (indices, tensor))."""
+    import torch
+    gen = torch.Generator(device=device).manual_seed(seed)
+    sizes = torch.randint(nmin, nmax + 1, (N,), generator=gen, device=device).cpu().numpy()
+    fam = np.arange(N) % 3
+    by_n = {}
+    for n in np.unique(sizes):
+        idx = np.nonzero(sizes == n)[0]
+        k = len(idx)
+        out = torch.empty(k, n, n, dtype=torch.complex128, device=device)
+        f = torch.from_numpy(fam[idx]).to(device)
+        g = f == 0
+        if g.any():
+            c = int(g.sum())
+            out[g] = torch.complex(torch.randn(c, n, n, generator=gen, dtype=torch.float64, device=device),
+                                   torch.randn(c, n, n, generator=gen, dtype=torch.float64, device=device))
+        g = f == 1
+        if g.any():
+            c = int(g.sum())
+            U, W = _haar(gen, c, n, device), _haar(gen, c, n, device)
+            s = torch.logspace(0, -4, n, dtype=torch.float64, device=device).to(torch.complex128)
+            V = (U * s[None, None, :]) @ W
+            r = torch.sqrt(torch.rand(c, n, generator=gen, dtype=torch.float64, device=device))
+            th = 2 * np.pi * torch.rand(c, n, generator=gen, dtype=torch.float64, device=device)
+            lam = torch.polar(r, th)
+            out[g] = (V * lam[:, None, :]) @ torch.linalg.inv(V)
+        g = f == 2
+        if g.any():
+            c = int(g.sum())
+            centres = torch.complex(torch.randn(c, 4, generator=gen, dtype=torch.float64, device=device),
+                                    torch.randn(c, 4, generator=gen, dtype=torch.float64, device=device))
+            r = 1e-6 * torch.sqrt(torch.rand(c, n, generator=gen, dtype=torch.float64, device=device))
+            th = 2 * np.pi * torch.rand(c, n, generator=gen, dtype=torch.float64, device=device)
+            lam = centres[:, torch.arange(n, device=device) % 4] + torch.polar(r, th)
+            G = torch.complex(torch.randn(c, n, n, generator=gen, dtype=torch.float64, device=device),
+                              torch.randn(c, n, n, generator=gen, dtype=torch.float64, device=device))
+            X = _haar(gen, c, n, device) + 0.3 * G
+            out[g] = (X * lam[:, None, :]) @ torch.linalg.inv(X)
+        by_n[int(n)] = (idx, out)
+    if not as_list:
+        return sizes, by_n
+    mats = [None] * N
+    for n, (idx, out) in by_n.items():
+        arr = out.cpu().numpy()
+        for j, i in enumerate(idx):
+            mats[i] = arr[j]
+    return mats
+
+
+def pack_varsize(sizes, by_n, device="cpu"):
+    """Packed mixed-size layout (ves_eigensolve_varsize): per matrix column-major
+    and contiguous, in index order.  Returns (dims int32, re, im) tensors."""
+    import torch
+    sizes = np.asarray(sizes)
+    off = np.concatenate([[0], np.cumsum(sizes.astype(np.int64) ** 2)])
+    total = int(off[-1])
+    re = torch.empty(total, dtype=torch.float64, device=device)
+    im = torch.empty(total, dtype=torch.float64, device=device)
+    for n, (idx, out) in by_n.items():
+        cm = out.transpose(1, 2).reshape(len(idx), n * n)  # column-major rows
+        pos = torch.from_numpy(off[idx]).to(device)[:, None] + torch.arange(n * n, device=device)[None, :]
+        re[pos.reshape(-1)] = cm.real.reshape(-1)
+        im[pos.reshape(-1)] = cm.imag.reshape(-1)
+    return torch.from_numpy(sizes.astype(np.int32)).to(device), re, im
