@@ -266,6 +266,176 @@ def measure_form(name, n, N, seed, tc, precision, warmup, steps):
     return out
 
 
+def _mat(re, im, n, tc):
+    import torch
+    return torch.complex(re.view(-1, n, n, tc).permute(0, 3, 2, 1), im.view(-1, n, n, tc).permute(0, 3, 2, 1)
+                         ).reshape(-1, n, n)
+
+
+def _vec(re, im, n, tc):
+    import torch
+    return torch.complex(re.view(-1, n, tc).permute(0, 2, 1), im.view(-1, n, tc).permute(0, 2, 1)).reshape(-1, n)
+
+
+def eig_distance(E1, E0, A, chunk=1 << 17):
+    """max over matrices and eigenvalues of the distance from each eigenvalue in
+    E1 to the nearest one in E0, relative to ||A||_F (device)."""
+    import torch
+    worst = 0.0
+    for s in range(0, E1.shape[0], chunk):
+        d = (E1[s:s + chunk, :, None] - E0[s:s + chunk, None, :]).abs().amin(dim=2)
+        nA = torch.linalg.matrix_norm(A[s:s + chunk])
+        worst = max(worst, float((d / nA[:, None]).max()))
+    return worst
+
+
+def measure_learned(n, N, train_count, epochs, steps, tc=512):
+    """The learned-shift form on the parametric family A(p) = A0 + p1 A1 + p2 A2
+    + p3 A3 (order n): the network is trained (tcgen05 BF16 MLP) on
+    `train_count` plain-solver solutions (param seed 5), then on a fresh batch
+    (param seed 6) one step = network inference + shift-seeded FP64 solve,
+    against the plain FP64 solve of the same batch."""
+    import torch
+    import ves
+    import learned_shift
+    t0 = time.perf_counter()
+    net, losses = learned_shift.train(n, count=train_count, epochs=epochs, batch=1024, lr=1e-3, hidden=256)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    p, rA, iA = learned_shift.family(N, n, param_seed=6, thread_cnt=tc)
+    bc = N // tc
+    rE0 = torch.empty(N * n, dtype=torch.float64, device="cuda")
+    iE0, rE, iE = torch.empty_like(rE0), torch.empty_like(rE0), torch.empty_like(rE0)
+    rS, iS = torch.empty_like(rE0), torch.empty_like(rE0)
+    rV, iV = torch.empty_like(rA), torch.empty_like(iA)
+    sw0, sw, st, fb = (torch.zeros(N, dtype=torch.int32, device="cuda") for _ in range(4))
+    ws = ves.Workspace(n, bc, tc)
+    pws = net.predict_workspace(N)
+    stream = torch.cuda.current_stream()
+
+    def plain(**kw):
+        ves.eigensolve(n, bc, tc, rA, iA, rE0, iE0, rV, iV, workspace=ws, stream=stream, **kw)
+
+    def learned(**kw):
+        net.predict_into(N, tc, p, rA, iA, rS, iS, pws, stream=stream)
+        ves.eigensolve_shifts(n, bc, tc, rA, iA, rE, iE, rV, iV, rS, iS, workspace=ws, stream=stream, **kw)
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    ms_plain = timed(plain)
+    ms_learned = timed(learned)
+    plain(sweeps=sw0)
+    learned(status=st, sweeps=sw, fallbacks=fb)
+    torch.cuda.synchronize()
+    ver = device_residual_check(rA, iA, rE, iE, rV, iV, n, tc)
+    A = _mat(rA, iA, n, tc)
+    err = eig_distance(_vec(rE, iE, n, tc), _vec(rE0, iE0, n, tc), A)
+    pred_err = (_vec(rS, iS, n, tc)[:, :, None] - _vec(rE0, iE0, n, tc)[:, None, :]).abs().amin(dim=2)
+    nA = torch.linalg.matrix_norm(A)
+    other = int(((st & ~4) != 0).sum())
+    out = {"form": "learned shift", "n": n, "n_matrices": N, "family": "A0 + p1 A1 + p2 A2 + p3 A3, p ~ U[-1,1]^3",
+           "value": N / (ms_learned * 1e-3), "unit": "eigensolves/s", "ms_per_step": ms_learned,
+           "plain_fp64_value": N / (ms_plain * 1e-3), "speedup_vs_plain": ms_plain / ms_learned,
+           "sweeps_per_eigenvalue": float(sw.double().mean()) / n,
+           "plain_sweeps_per_eigenvalue": float(sw0.double().mean()) / n,
+           "fallback_per_eigenvalue": float(fb.double().mean()) / n,
+           "prediction_error_median_rel": float((pred_err / nA[:, None]).median()),
+           "train": {"matrices": train_count, "epochs": epochs, "seconds": train_s, "loss_first": losses[0],
+                     "loss_last": losses[-1]},
+           "max_residual": ver["max_residual"], "nonfinite": ver["nonfinite"], "max_eig_err_rel": err,
+           "passed": ver["max_residual"] <= RES_TOL and ver["nonfinite"] == 0 and err <= 1e-12 and other == 0}
+    del net, rA, iA, rV, iV, ws, pws, A
+    torch.cuda.empty_cache()
+    return out
+
+
+def measure_varsize(count, steps, seed=2, max_dim=64):
+    """Mixed-size batch (orders uniform in [4, 64]; Gaussian, non-normal and
+    clustered families): one persistent size-binned launch (ves_eigensolve_varsize,
+    replayed as a CUDA graph) against one ves_eigensolve launch per order."""
+    import torch
+    import ves
+    import workloads
+    sizes, by_n = workloads.mixed_families(count, seed=seed, nmax=max_dim, device="cuda", as_list=False)
+    dims, re, im = workloads.pack_varsize(sizes, by_n, device="cuda")
+    er = torch.empty(int(sizes.sum()), dtype=torch.float64, device="cuda")
+    ei = torch.empty_like(er)
+    vr, vi = torch.empty_like(re), torch.empty_like(im)
+    st = torch.zeros(count, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    o = ves.default_options()
+    g = ves.VarsizeGraph(count, max_dim, dims, re, im, er, ei, vr, vi, status=st, options=o)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms = timed(lambda: g.launch(stream), steps)
+    bad = int((st != 0).sum())
+    # residuals per order bucket (packed column-major per matrix)
+    off = np.concatenate([[0], np.cumsum(sizes.astype(np.int64) ** 2)])
+    eoff = np.concatenate([[0], np.cumsum(sizes.astype(np.int64))])
+    worst = 0.0
+    per_n = []
+    for n, (idx, _) in sorted(by_n.items()):
+        ii = torch.from_numpy(idx).cuda()
+        o2 = torch.from_numpy(off[idx]).cuda()[:, None] + torch.arange(n * n, device="cuda")[None]
+        e2 = torch.from_numpy(eoff[idx]).cuda()[:, None] + torch.arange(n, device="cuda")[None]
+        A = torch.complex(re[o2], im[o2]).view(-1, n, n).transpose(1, 2)
+        V = torch.complex(vr[o2], vi[o2]).view(-1, n, n).transpose(1, 2)
+        E = torch.complex(er[e2], ei[e2])
+        r = torch.linalg.vector_norm(A @ V - V * E[:, None, :], dim=1)
+        q = r / (torch.linalg.matrix_norm(A)[:, None] * torch.linalg.vector_norm(V, dim=1))
+        worst = max(worst, float(torch.nan_to_num(q, nan=1.0).max()))
+        # the per-order baseline: this bucket as its own SoA batch (thread_cnt = bucket size)
+        k = len(idx)
+        rs = A.real.permute(2, 1, 0).contiguous().reshape(-1)
+        is_ = A.imag.permute(2, 1, 0).contiguous().reshape(-1)
+        per_n.append((n, k, rs, is_))
+        del ii
+    del A, V
+    bufs = []
+    need = 0
+    for n, k, rs, is_ in per_n:
+        eb = torch.empty(k * n, dtype=torch.float64, device="cuda")
+        bufs.append((n, k, rs, is_, eb, torch.empty_like(eb), torch.empty_like(rs), torch.empty_like(is_)))
+        need = max(need, ves.lib().ves_eigensolve_workspace_size(n, 1, k, ves.ctypes.byref(o)))
+    w = ves.DeviceBuffer(need)  # launches are stream-ordered: one workspace serves all orders
+
+    def per_order():
+        for n, k, rs, is_, eb, eb2, vb, vb2 in bufs:
+            ves.eigensolve(n, 1, k, rs, is_, eb, eb2, vb, vb2, workspace=w, stream=stream)
+
+    ms_per_order = timed(per_order, max(1, steps // 2))
+    out = {"form": "mixed-size batch", "n_matrices": count, "orders": "uniform in [4, %d]" % max_dim,
+           "families": "Gaussian / non-normal (cond(V)=1e4) / clustered (4 centres, radius 1e-6)",
+           "value": count / (ms * 1e-3), "unit": "eigensolves/s", "ms_per_step": ms,
+           "api": "ves_eigensolve_varsize captured in a CUDA graph, replayed",
+           "per_order_launches_value": count / (ms_per_order * 1e-3),
+           "speedup_vs_per_order_launches": ms_per_order / ms, "max_residual": worst, "status_nonzero": bad,
+           "passed": worst <= RES_TOL and bad == 0}
+    del g, bufs, per_n, re, im, vr, vi, er, ei, w
+    torch.cuda.empty_cache()
+    return out
+
+
 def flops_per_matrix(n, s):
     return 24.0 * n ** 3 + 20.0 * s * n ** 3
 
@@ -363,6 +533,11 @@ def run_gpu_arm(args, d):
         m32 = measure_form("FP32+refine", 32, 262_144, 3, 512, 1, 1, 2)
         m32["speedup_vs_plain"] = m32["value"] / p32["value"]
         forms += [p32, m32]
+        for ln in (16, 32):
+            log("[bench] learned-shift form, n=%d" % ln)
+            forms.append(measure_learned(ln, 262_144, 200_000, 20, 2))
+        log("[bench] mixed-size form")
+        forms.append(measure_varsize(500_000, 2))
 
     d.done()
     if d.rank != 0:
@@ -466,7 +641,8 @@ def main():
     ap.add_argument("--impl", default="ves", choices=["ves", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-forms", action="store_true", help="skip the FP32+refine and n=32 lines")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the FP32+refine, n=32, learned-shift and mixed-size lines")
     ap.add_argument("--ncu-case", type=int, default=0, metavar="N",
                     help="no benchmark: one solve per form on N matrices (for ncu captures)")
     ap.add_argument("--ncu-n", type=int, default=16)

@@ -132,17 +132,20 @@ struct WsPlan {
     size_t fp64, mixed, list, count, total;
 };
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
-WsPlan workspace_plan(int precision, int n, long long N, bool vectors = true)
+WsPlan workspace_plan(int precision, int n, long long N, bool vectors, int bps)
 {
     WsPlan p{};
     if (!vectors) {
-        p.fp64 = align256(ves::eigvals_workspace_bytes(n, N));
+        p.fp64 = align256(ves::eigvals_workspace_bytes(n, N, bps));
         p.total = p.fp64;
         return p;
     }
-    p.fp64 = align256(ves::fused_workspace_bytes(n, N, nullptr, nullptr));
-    if (precision == VES_PREC_FP32_REFINE) {
-        p.mixed = align256(ves::mixed_workspace_bytes(n, N, nullptr, nullptr));
+    // FP64: blocks_per_sm shapes the fused kernel; FP32 + refinement: it shapes
+    // the FP32 Schur kernel and the FP64 fallback pass keeps the default grid
+    const bool mixed = precision == VES_PREC_FP32_REFINE;
+    p.fp64 = align256(ves::fused_workspace_bytes(n, N, mixed ? 0 : bps, nullptr, nullptr));
+    if (mixed) {
+        p.mixed = align256(ves::mixed_workspace_bytes(n, N, bps, nullptr, nullptr));
         p.list = align256((size_t)N * sizeof(int));
         p.count = 256;
     }
@@ -164,7 +167,7 @@ bool do_eigensolver(int dim, int bc, int tc, double *rA, double *iA, double *rE,
     double *dAr = b.d(0, nm), *dAi = b.d(1, nm), *dVr = b.d(2, nm), *dVi = b.d(3, nm);
     double *dEr = b.d(4, nv), *dEi = b.d(5, nv);
     NEED(dAr); NEED(dAi); NEED(dVr); NEED(dVi); NEED(dEr); NEED(dEi);
-    const size_t wsb = ves::fused_workspace_bytes(dim, g.N, nullptr, nullptr);
+    const size_t wsb = ves::fused_workspace_bytes(dim, g.N, 0, nullptr, nullptr);
     void *ws = b.raw(6, wsb);
     NEED(ws);
     if (!h2d(dAr, rA, nm * 8) || !h2d(dAi, iA, nm * 8)) return false;
@@ -429,7 +432,7 @@ size_t ves_eigensolve_workspace_size(int dim, int block_cnt, int thread_cnt, con
     ves_options o;
     ves_default_options(&o);
     if (opt) o = *opt;
-    return workspace_plan(o.precision, dim, g.N, o.want_vectors != 0).total;
+    return workspace_plan(o.precision, dim, g.N, o.want_vectors != 0, o.blocks_per_sm).total;
 }
 
 int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, const double *iA, double *rE, double *iE,
@@ -466,11 +469,15 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
     }
     if (o.max_its < 0 || o.max_its > 10000) { set_error("max_its=%d outside [0, 10000]", o.max_its); return VES_ERR_ARG; }
     if (o.vnorm < 0 || o.vnorm > 2) { set_error("vnorm=%d unknown", o.vnorm); return VES_ERR_ARG; }
+    if (o.blocks_per_sm < 0 || o.blocks_per_sm > 16) {
+        set_error("blocks_per_sm=%d outside [0, 16]", o.blocks_per_sm);
+        return VES_ERR_ARG;
+    }
     if (o.refine_steps < 0 || o.refine_steps > 100 || !(o.refine_tol > 0.0)) {
         set_error("refine_steps=%d / refine_tol=%g out of range", o.refine_steps, o.refine_tol);
         return VES_ERR_ARG;
     }
-    const WsPlan plan = workspace_plan(o.precision, dim, g.N, vectors);
+    const WsPlan plan = workspace_plan(o.precision, dim, g.N, vectors, o.blocks_per_sm);
     const size_t need = plan.total;
     void *ws = workspace;
     std::unique_lock<std::mutex> lk;
@@ -492,10 +499,12 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
     a.ws = ws;
     a.max_its = o.max_its;
     a.vnorm = o.vnorm;
+    a.blocks_per_sm = o.precision == VES_PREC_FP64 ? o.blocks_per_sm : 0;
     cudaStream_t st = (cudaStream_t)stream;
     if (!vectors)
-        return native(cuda_ok(ves::launch_eigvals(g, rA, iA, rE, iE, status, sweeps, ws, o.max_its, st),
-                              "eigenvalues kernel launch"));
+        return native(cuda_ok(
+            ves::launch_eigvals(g, rA, iA, rE, iE, status, sweeps, ws, o.max_its, o.blocks_per_sm, st),
+            "eigenvalues kernel launch"));
     if (o.precision == VES_PREC_FP64)
         return native(cuda_ok(ves::launch_fused_fp64(a, st), "eigensolve kernel launch"));
 
@@ -516,6 +525,7 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
     m.tol = o.refine_tol;
     m.fb_list = list;
     m.fb_count = count;
+    m.blocks_per_sm = o.blocks_per_sm;
     if (!cuda_ok(ves::launch_mixed(m, st), "mixed-precision kernel launch")) return VES_ERR_CUDA;
     a.list = list;
     a.list_count = count;
@@ -526,7 +536,7 @@ size_t ves_polyroots_workspace_size(int degree, int block_cnt, int thread_cnt)
 {
     ves::Geom g;
     if (!geom_ok(degree, block_cnt, thread_cnt, &g)) return 0;
-    return align256(ves::eigvals_workspace_bytes(degree, g.N));
+    return align256(ves::eigvals_workspace_bytes(degree, g.N, 0));
 }
 
 int ves_polyroots(int degree, int block_cnt, int thread_cnt, const double *rC, const double *iC, double *rR,
@@ -537,7 +547,7 @@ int ves_polyroots(int degree, int block_cnt, int thread_cnt, const double *rC, c
     if (!geom_ok(degree, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
     if (g.N == 0) return VES_OK;
     if (!rC || !iC || !rR || !iR) { set_error("null pointer"); return VES_ERR_ARG; }
-    const size_t need = align256(ves::eigvals_workspace_bytes(degree, g.N));
+    const size_t need = align256(ves::eigvals_workspace_bytes(degree, g.N, 0));
     void *ws = workspace;
     std::unique_lock<std::mutex> lk;
     if (!ws) {
@@ -611,11 +621,11 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *
     ves_default_options(&o);
     if (opt) o = *opt;
     if (o.max_its < 0 || o.max_its > 10000 || o.vnorm < 0 || o.vnorm > 2 || o.shift_sweeps < 0 ||
-        o.shift_sweeps > 9) {
+        o.shift_sweeps > 9 || o.blocks_per_sm < 0 || o.blocks_per_sm > 16) {
         set_error("option out of range");
         return VES_ERR_ARG;
     }
-    const size_t need = align256(ves::fused_workspace_bytes(dim, g.N, nullptr, nullptr));
+    const size_t need = align256(ves::fused_workspace_bytes(dim, g.N, o.blocks_per_sm, nullptr, nullptr));
     void *ws = workspace;
     std::unique_lock<std::mutex> lk;
     if (!ws) {
@@ -636,6 +646,7 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *
     a.rS = rS; a.iS = iS;
     a.shift_sweeps = o.shift_sweeps;
     a.fallbacks = fallbacks;
+    a.blocks_per_sm = o.blocks_per_sm;
     return native(cuda_ok(ves::launch_fused_fp64(a, (cudaStream_t)stream), "learned-shift solve launch"));
 }
 
@@ -657,7 +668,7 @@ int ves_gemm_bf16(int M, int N, int K, const void *A, int lda, const void *Bt, i
                           "gemm launch"));
 }
 
-static int varsize_bps(const ves_options &o) { return o.blocks_per_sm > 0 ? o.blocks_per_sm : 2; }
+static int varsize_bps(const ves_options &o) { return o.blocks_per_sm > 0 ? o.blocks_per_sm : 4; }
 
 size_t ves_eigensolve_varsize_workspace_size(long long count, int max_dim, const ves_options *opt)
 {

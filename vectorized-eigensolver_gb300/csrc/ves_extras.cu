@@ -171,28 +171,29 @@ __global__ void soa_to_aos_kernel(const double *re, const double *im, double2 *Z
 
 int g_extras_blocks_per_sm = 2;
 
-long long persistent_blocks(long long N)
+long long persistent_blocks(long long N, int blocks_per_sm)
 {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
     const long long groups = (N + 31) / 32;
-    return std::max<long long>(1, std::min<long long>((groups + 3) / 4, (long long)sms * g_extras_blocks_per_sm));
+    return std::max<long long>(1, std::min<long long>((groups + 3) / 4, (long long)sms * (blocks_per_sm > 0 ? blocks_per_sm : g_extras_blocks_per_sm)));
 }
 
 }  // namespace
 
-size_t eigvals_workspace_bytes(int n, long long N)
+size_t eigvals_workspace_bytes(int n, long long N, int blocks_per_sm)
 {
-    return (size_t)persistent_blocks(N) * 4 * ((size_t)n * n + n) * 32 * sizeof(double2);
+    return (size_t)persistent_blocks(N, blocks_per_sm) * 4 * ((size_t)n * n + n) * 32 * sizeof(double2);
 }
 
 cudaError_t launch_eigvals(Geom g, const double *rA, const double *iA, double *rE, double *iE, int *status,
-                           int *sweeps, void *ws, int max_its, cudaStream_t st)
+                           int *sweeps, void *ws, int max_its, int blocks_per_sm, cudaStream_t st)
 {
     if (g.N <= 0) return cudaSuccess;
-    eigvals_fp64_kernel<<<(unsigned)persistent_blocks(g.N), kThreads, 0, st>>>(g, rA, iA, rE, iE, status, sweeps, ws,
+    eigvals_fp64_kernel<<<(unsigned)persistent_blocks(g.N, blocks_per_sm), kThreads, 0, st>>>(g, rA, iA, rE, iE,
+                                                                                              status, sweeps, ws,
                                                                                max_its);
     return cudaGetLastError();
 }
@@ -201,7 +202,7 @@ cudaError_t launch_polyroots(Geom g, const double *rC, const double *iC, double 
                              void *ws, int max_its, cudaStream_t st)
 {
     if (g.N <= 0) return cudaSuccess;
-    polyroots_kernel<<<(unsigned)persistent_blocks(g.N), kThreads, 0, st>>>(g, rC, iC, rR, iR, status, ws, max_its);
+    polyroots_kernel<<<(unsigned)persistent_blocks(g.N, 0), kThreads, 0, st>>>(g, rC, iC, rR, iR, status, ws, max_its);
     return cudaGetLastError();
 }
 

@@ -36,6 +36,7 @@ struct FusedArgs {
     const double *rS, *iS;
     int shift_sweeps;
     int *fallbacks;
+    int blocks_per_sm;  // persistent grid: blocks (4 warps) per SM; 0 = default
 };
 
 struct MixedArgs {
@@ -52,13 +53,15 @@ struct MixedArgs {
     double tol;     // ||r|| <= tol ||A||_F ||v||
     int *fb_list;   // matrices handed to the FP64 solver
     int *fb_count;
+    int blocks_per_sm;  // FP32 Schur kernel grid: blocks per SM; 0 = default
 };
 
-size_t mixed_workspace_bytes(int n, long long N, int *out_blocks, int *out_threads);
+size_t mixed_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blocks, int *out_threads);
 cudaError_t launch_mixed(const MixedArgs &a, cudaStream_t st);
 
 // Fused zgehrd -> zunghr -> zlahqr -> ztrevc, FP64.
-size_t fused_workspace_bytes(int n, long long N, int *out_blocks, int *out_threads);
+// blocks_per_sm = 0 takes the library default (VES_FUSED_BLOCKS_PER_SM, else 2).
+size_t fused_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blocks, int *out_threads);
 cudaError_t launch_fused_fp64(const FusedArgs &a, cudaStream_t st);
 
 // Stage kernels, in place on the SoA layout (reference call_* semantics).
@@ -80,9 +83,9 @@ cudaError_t launch_fused_fp64_blocks(const FusedArgs &a, int blocks, cudaStream_
 
 // Eigenvalues only (no Q, no Schur vectors), companion-matrix roots, and the
 // SoA <-> interleaved-complex transposes.
-size_t eigvals_workspace_bytes(int n, long long N);
+size_t eigvals_workspace_bytes(int n, long long N, int blocks_per_sm);
 cudaError_t launch_eigvals(Geom g, const double *rA, const double *iA, double *rE, double *iE, int *status,
-                           int *sweeps, void *ws, int max_its, cudaStream_t st);
+                           int *sweeps, void *ws, int max_its, int blocks_per_sm, cudaStream_t st);
 cudaError_t launch_polyroots(Geom g, const double *rC, const double *iC, double *rR, double *iR, int *status,
                              void *ws, int max_its, cudaStream_t st);
 cudaError_t launch_transpose(bool to_soa, const double *src_re, const double *src_im, double *dst_re, double *dst_im,

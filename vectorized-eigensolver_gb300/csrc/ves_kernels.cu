@@ -248,7 +248,7 @@ int g_fused_blocks_per_sm = 2;  // 8 warps per SM; tunable through VES_FUSED_BLO
 
 }  // namespace
 
-size_t fused_workspace_bytes(int n, long long N, int *out_blocks, int *out_threads)
+size_t fused_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blocks, int *out_threads)
 {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -264,7 +264,8 @@ size_t fused_workspace_bytes(int n, long long N, int *out_blocks, int *out_threa
     }
     const long long groups = (N + 31) / 32;
     const int wpb = kFusedThreads / 32;
-    long long blocks = std::min<long long>((groups + wpb - 1) / wpb, (long long)sms * g_fused_blocks_per_sm);
+    const int bps = blocks_per_sm > 0 ? blocks_per_sm : g_fused_blocks_per_sm;
+    long long blocks = std::min<long long>((groups + wpb - 1) / wpb, (long long)sms * bps);
     if (blocks < 1) blocks = 1;
     const size_t per_slot = (size_t)(2LL * n * n + n) * 32 * sizeof(double2);
     if (out_blocks) *out_blocks = (int)blocks;
@@ -276,7 +277,7 @@ cudaError_t launch_fused_fp64(const FusedArgs &a, cudaStream_t st)
 {
     if (a.g.N <= 0) return cudaSuccess;
     int blocks = 0, threads = 0;
-    fused_workspace_bytes(a.g.n, a.g.N, &blocks, &threads);
+    fused_workspace_bytes(a.g.n, a.g.N, a.blocks_per_sm, &blocks, &threads);
     if (a.rS)
         fused_fp64_kernel<true><<<blocks, threads, 0, st>>>(a);
     else

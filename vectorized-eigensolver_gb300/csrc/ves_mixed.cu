@@ -232,9 +232,9 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
     for (int i = 1; i <= n; ++i) Vo.st(i, k, cscal(v[i - 1], scale));
 }
 
-int g_schur_blocks_per_sm = 4;
+int g_schur_blocks_per_sm = 8;
 
-long long schur_blocks(long long N)
+long long schur_blocks(long long N, int blocks_per_sm)
 {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -249,15 +249,16 @@ long long schur_blocks(long long N)
         }
     }
     const long long groups = (N + 31) / 32;
-    return std::max<long long>(1, std::min<long long>((groups + 3) / 4, (long long)sms * g_schur_blocks_per_sm));
+    const int bps = blocks_per_sm > 0 ? blocks_per_sm : g_schur_blocks_per_sm;
+    return std::max<long long>(1, std::min<long long>((groups + 3) / 4, (long long)sms * bps));
 }
 
 }  // namespace
 
-size_t mixed_workspace_bytes(int n, long long N, int *out_blocks, int *out_threads)
+size_t mixed_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blocks, int *out_threads)
 {
     const long long groups = (N + 31) / 32;
-    if (out_blocks) *out_blocks = (int)schur_blocks(N);
+    if (out_blocks) *out_blocks = (int)schur_blocks(N, blocks_per_sm);
     if (out_threads) *out_threads = kSchurThreads;
     const size_t bufb = (size_t)groups * group_elems(n) * 32 * sizeof(float2);
     const size_t flagb = ((size_t)N * sizeof(int) + 255) & ~(size_t)255;
@@ -273,7 +274,7 @@ cudaError_t launch_mixed(const MixedArgs &a, cudaStream_t st)
     float2 *buf = static_cast<float2 *>(a.ws);
     int *flags = reinterpret_cast<int *>(static_cast<char *>(a.ws) +
                                          (size_t)groups * group_elems(n) * 32 * sizeof(float2));
-    schur32_kernel<<<(unsigned)schur_blocks(a.g.N), kSchurThreads, 0, st>>>(a, buf, flags);
+    schur32_kernel<<<(unsigned)schur_blocks(a.g.N, a.blocks_per_sm), kSchurThreads, 0, st>>>(a, buf, flags);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const long long pairs = a.g.N * n;

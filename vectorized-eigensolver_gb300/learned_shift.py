@@ -17,8 +17,11 @@ import ves
 
 
 def family(N, n, family_seed=4, param_seed=5, thread_cnt=512, device="cuda"):
-    """Returns (params (N, 3) float64, rA, iA SoA planes) on `device`."""
+    """Returns (params (N, 3) float64, rA, iA SoA planes) on `device`; N must be
+    a multiple of thread_cnt."""
     import torch
+    if N % thread_cnt:
+        raise ValueError("N=%d is not a multiple of thread_cnt=%d" % (N, thread_cnt))
     g = torch.Generator(device=device).manual_seed(family_seed)
     basis = torch.complex(torch.randn(4, n, n, generator=g, dtype=torch.float64, device=device),
                           torch.randn(4, n, n, generator=g, dtype=torch.float64, device=device)) / np.sqrt(n)
@@ -46,8 +49,10 @@ def solve_plain(n, N, rA, iA, thread_cnt=512, vectors=False):
 
 def train(n, count=200_000, epochs=30, batch=1024, lr=1e-3, hidden=256, family_seed=4, param_seed=5, seed=0,
           thread_cnt=512):
-    """Train a ShiftNet for order n on `count` plain-solver solutions."""
+    """Train a ShiftNet for order n on `count` plain-solver solutions (rounded
+    down to a multiple of thread_cnt)."""
     import torch
+    count = max(thread_cnt, count // thread_cnt * thread_cnt)
     p, rA, iA = family(count, n, family_seed, param_seed, thread_cnt)
     rE, iE, _ = solve_plain(n, count, rA, iA, thread_cnt)
     torch.cuda.synchronize()

@@ -396,11 +396,18 @@ class ShiftNet:
                "ves_shiftnet_train")
         return list(losses)[:epochs]
 
-    def predict(self, count, thread_cnt, params, rA, iA, rS, iS, stream=None):
-        ws = DeviceBuffer(lib().ves_shiftnet_predict_workspace_size(self.handle, count))
+    def predict_workspace(self, count):
+        return DeviceBuffer(lib().ves_shiftnet_predict_workspace_size(self.handle, count))
+
+    def predict_into(self, count, thread_cnt, params, rA, iA, rS, iS, workspace, stream=None):
+        """Inference into rS, iS with a caller-held workspace (predict_workspace)."""
         _check(lib().ves_shiftnet_predict(self.handle, count, thread_cnt, _dp(params), _dp(rA), _dp(iA), _dp(rS),
-                                          _dp(iS), ctypes.c_void_p(ws.ptr), ws.nbytes, _stream_ptr(stream)),
-               "ves_shiftnet_predict")
+                                          _dp(iS), ctypes.c_void_p(workspace.ptr), workspace.nbytes,
+                                          _stream_ptr(stream)), "ves_shiftnet_predict")
+
+    def predict(self, count, thread_cnt, params, rA, iA, rS, iS, stream=None):
+        ws = self.predict_workspace(count)
+        self.predict_into(count, thread_cnt, params, rA, iA, rS, iS, ws, stream)
         return ws
 
     def save(self, path):

@@ -60,13 +60,28 @@ def gaussian_soa(N, n, seed, thread_cnt):
     return planes[0], planes[1]
 
 
-def _haar(gen, k, n, device):
+def _unitary(gen, k, n, device):
+    """k random dense unitaries H(u) H(w) diag(phases), H(x) = I - 2 x x^H / |x|^2:
+    cheap to form (no factorisation), dense, exactly unitary."""
     import torch
-    G = torch.complex(torch.randn(k, n, n, generator=gen, dtype=torch.float64, device=device),
-                      torch.randn(k, n, n, generator=gen, dtype=torch.float64, device=device))
-    Q, R = torch.linalg.qr(G)
-    d = torch.diagonal(R, dim1=1, dim2=2)
-    return Q * (d / d.abs().clamp_min(1e-300))[:, None, :]  # Haar-distributed unitary
+
+    def refl():
+        x = torch.complex(torch.randn(k, n, generator=gen, dtype=torch.float64, device=device),
+                          torch.randn(k, n, generator=gen, dtype=torch.float64, device=device))
+        x = x / torch.linalg.vector_norm(x, dim=1, keepdim=True)
+        return torch.eye(n, dtype=torch.complex128, device=device)[None] - 2 * x[:, :, None] * x.conj()[:, None, :]
+
+    ph = torch.polar(torch.ones(k, n, dtype=torch.float64, device=device),
+                     2 * np.pi * torch.rand(k, n, generator=gen, dtype=torch.float64, device=device))
+    return (refl() @ refl()) * ph[:, None, :]
+
+
+def _similar(U, s, W, lam):
+    """A = (U diag(s) W) diag(lam) (U diag(s) W)^-1, the inverse taken exactly as
+    W^H diag(1/s) U^H because U and W are unitary."""
+    V = (U * s[None, None, :]) @ W
+    Vinv = (W.conj().transpose(1, 2) * (1.0 / s)[None, None, :]) @ U.conj().transpose(1, 2)
+    return (V * lam[:, None, :]) @ Vinv
 
 
 def mixed_families(N, seed=2, nmin=4, nmax=64, device="cpu", as_list=True):
@@ -74,11 +89,13 @@ def mixed_families(N, seed=2, nmin=4, nmax=64, device="cpu", as_list=True):
     [nmin, nmax], matrix m of family m % 3:
       0  i.i.d. complex Gaussian;
       1  non-normal A = V diag(l) V^-1, V = U diag(logspace(0, -4, n)) W with U, W
-         Haar unitary (cond(V) = 1e4), l uniform in the unit disk;
-      2  clustered A = X diag(l) X^-1, l = one of 4 complex-Gaussian centres plus
-         an offset uniform in a disk of radius 1e-6, X = U + 0.3 G (U Haar).
-    Generated with torch (seeded), batched by order.  Returns a list of (n, n)
-    numpy arrays (as_list) or (sizes, dict n -> (indices, tensor))."""
+         random dense unitaries (cond(V) = 1e4), l uniform in the unit disk;
+      2  clustered A = X diag(l) X^-1, X = U diag(logspace(0, -1, n)) W (cond 10),
+         l = one of 4 complex-Gaussian centres plus an offset uniform in a disk of
+         radius 1e-6.
+    Generated with torch (seeded), batched by order, matrix products only.
+    Returns a list of (n, n) numpy arrays (as_list) or (sizes, dict n -> (indices,
+    tensor))."""
     import torch
     gen = torch.Generator(device=device).manual_seed(seed)
     sizes = torch.randint(nmin, nmax + 1, (N,), generator=gen, device=device).cpu().numpy()
@@ -97,13 +114,10 @@ def mixed_families(N, seed=2, nmin=4, nmax=64, device="cpu", as_list=True):
         g = f == 1
         if g.any():
             c = int(g.sum())
-            U, W = _haar(gen, c, n, device), _haar(gen, c, n, device)
             s = torch.logspace(0, -4, n, dtype=torch.float64, device=device).to(torch.complex128)
-            V = (U * s[None, None, :]) @ W
             r = torch.sqrt(torch.rand(c, n, generator=gen, dtype=torch.float64, device=device))
             th = 2 * np.pi * torch.rand(c, n, generator=gen, dtype=torch.float64, device=device)
-            lam = torch.polar(r, th)
-            out[g] = (V * lam[:, None, :]) @ torch.linalg.inv(V)
+            out[g] = _similar(_unitary(gen, c, n, device), s, _unitary(gen, c, n, device), torch.polar(r, th))
         g = f == 2
         if g.any():
             c = int(g.sum())
@@ -112,10 +126,8 @@ def mixed_families(N, seed=2, nmin=4, nmax=64, device="cpu", as_list=True):
             r = 1e-6 * torch.sqrt(torch.rand(c, n, generator=gen, dtype=torch.float64, device=device))
             th = 2 * np.pi * torch.rand(c, n, generator=gen, dtype=torch.float64, device=device)
             lam = centres[:, torch.arange(n, device=device) % 4] + torch.polar(r, th)
-            G = torch.complex(torch.randn(c, n, n, generator=gen, dtype=torch.float64, device=device),
-                              torch.randn(c, n, n, generator=gen, dtype=torch.float64, device=device))
-            X = _haar(gen, c, n, device) + 0.3 * G
-            out[g] = (X * lam[:, None, :]) @ torch.linalg.inv(X)
+            s = torch.logspace(0, -1, n, dtype=torch.float64, device=device).to(torch.complex128)
+            out[g] = _similar(_unitary(gen, c, n, device), s, _unitary(gen, c, n, device), lam)
         by_n[int(n)] = (idx, out)
     if not as_list:
         return sizes, by_n
