@@ -389,6 +389,11 @@ def measure_varsize(count, steps, seed=2, max_dim=64):
 
     ms = timed(lambda: g.launch(stream), steps)
     bad = int((st != 0).sum())
+    sw = torch.zeros(count, dtype=torch.int32, device="cuda")
+    ves.eigensolve_varsize(count, max_dim, dims, re, im, er, ei, vr, vi, sweeps=sw, options=o)
+    torch.cuda.synchronize()
+    nd = torch.from_numpy(sizes.astype(np.float64)).cuda()
+    flops = float((24.0 * nd ** 3 + 20.0 * sw.double() * nd ** 2).sum())
     # residuals per order bucket (packed column-major per matrix)
     off = np.concatenate([[0], np.cumsum(sizes.astype(np.int64) ** 2)])
     eoff = np.concatenate([[0], np.cumsum(sizes.astype(np.int64))])
@@ -428,6 +433,8 @@ def measure_varsize(count, steps, seed=2, max_dim=64):
            "families": "Gaussian / non-normal (cond(V)=1e4) / clustered (4 centres, radius 1e-6)",
            "value": count / (ms * 1e-3), "unit": "eigensolves/s", "ms_per_step": ms,
            "api": "ves_eigensolve_varsize captured in a CUDA graph, replayed",
+           "algorithmic_tflops": flops / (ms * 1e-3) / 1e12,
+           "sweeps_per_eigenvalue": float(sw.double().sum()) / float(nd.sum()),
            "per_order_launches_value": count / (ms_per_order * 1e-3),
            "speedup_vs_per_order_launches": ms_per_order / ms, "max_residual": worst, "status_nonzero": bad,
            "passed": worst <= RES_TOL and bad == 0}
@@ -615,10 +622,35 @@ def run_e2e(args, rA, iA, n, bc, tc, N):
 
 def run_ncu_case(args):
     """One solve per form on a small batch (inputs still larger than L2), no
-    timing: the case the ncu captures under profiles/ are taken on."""
+    timing: the case the ncu captures under profiles/ are taken on.
+    --ncu-form solve:    FP64 then FP32+refine on N Gaussian n x n matrices;
+    --ncu-form shiftnet: network inference (4 tcgen05 GEMMs) on N family matrices
+                         (untrained weights: the kernels do the same work);
+    --ncu-form varsize:  one mixed-size solve of N family matrices (orders 4..64)."""
     import torch
     import ves
     n, N, tc = args.ncu_n, args.ncu_case, 512
+    if args.ncu_form == "shiftnet":
+        import learned_shift
+        p, rA, iA = learned_shift.family(N, n, param_seed=6, thread_cnt=tc)
+        net = ves.ShiftNet(dim=n, n_params=3, hidden=256, seed=0)
+        rS = torch.empty(N * n, dtype=torch.float64, device="cuda")
+        iS = torch.empty_like(rS)
+        net.predict(N, tc, p, rA, iA, rS, iS)
+        torch.cuda.synchronize()
+        print("ncu case done: shift network inference on %d matrices, n=%d" % (N, n))
+        return
+    if args.ncu_form == "varsize":
+        import workloads
+        sizes, by_n = workloads.mixed_families(N, seed=2, device="cuda", as_list=False)
+        dims, re, im = workloads.pack_varsize(sizes, by_n, device="cuda")
+        er = torch.empty(int(sizes.sum()), dtype=torch.float64, device="cuda")
+        ei = torch.empty_like(er)
+        vr, vi = torch.empty_like(re), torch.empty_like(im)
+        ves.eigensolve_varsize(N, 64, dims, re, im, er, ei, vr, vi)
+        torch.cuda.synchronize()
+        print("ncu case done: mixed-size solve of %d matrices" % N)
+        return
     g = torch.Generator(device="cuda").manual_seed(1)
     rA = torch.randn(N * n * n, dtype=torch.float64, device="cuda", generator=g)
     iA = torch.randn(N * n * n, dtype=torch.float64, device="cuda", generator=g)
@@ -646,6 +678,7 @@ def main():
     ap.add_argument("--ncu-case", type=int, default=0, metavar="N",
                     help="no benchmark: one solve per form on N matrices (for ncu captures)")
     ap.add_argument("--ncu-n", type=int, default=16)
+    ap.add_argument("--ncu-form", default="solve", choices=["solve", "shiftnet", "varsize"])
     args = ap.parse_args()
     if args.ncu_case:
         run_ncu_case(args)

@@ -128,7 +128,10 @@ typedef struct ves_options {
     int blocks_per_sm; /* launch shape of the persistent kernels (4 warps per block); 0 = library default */
     int varsize_order; /* mixed-size batches: 0 (default) largest order first, 1 smallest first */
     int shift_sweeps;  /* ves_eigensolve_shifts: sweeps per eigenvalue that use a predicted shift; default 1 */
-    int reserved[2];
+    float shift_gate;  /* ves_eigensolve_shifts: an eigenvalue uses the predictions only while its subdiagonal
+                        * |H(I,I-1)| exceeds shift_gate * ||A||_F / sqrt(n) (below that the Wilkinson shift
+                        * is the better estimate); set it to the predictor's typical error; default 0 */
+    int reserved;
 } ves_options;
 
 void ves_default_options(ves_options *opt);
@@ -202,11 +205,30 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt,
                           const ves_options *opt, void *workspace, size_t workspace_bytes, void *stream);
 
 /* The shift network: features [family parameters (n_params per matrix, a
- * row-major FP64 device array), Re diag A, Im diag A] -> n predicted
- * eigenvalues; hidden layers of `hidden` units (multiple of 16, <= 256), GELU,
- * BF16 on the tcgen05 tensor cores.  Trained on eigenvalues from the FP64
- * solver (rE, iE in the SoA layout of rA, iA).  Checkpoints are flat binary. */
+ * row-major FP64 device array), optional sin/cos features of them, Re diag A,
+ * Im diag A] -> n predicted eigenvalues; hidden layers of `hidden` units, GELU,
+ * BF16 on the tcgen05 tensor cores; an FP32 output layer.  Trained on eigenvalues from the FP64
+ * solver (rE, iE in the SoA layout of rA, iA) with a permutation-invariant
+ * loss (symmetric Chamfer distance between the predicted and the true
+ * eigenvalue sets), Adam with cosine learning-rate decay from lr to lr/50 over
+ * the call's epochs.  Checkpoints are flat binary. */
 typedef struct ves_shiftnet ves_shiftnet;
+enum { VES_SHIFTNET_LOSS_CHAMFER = 0, VES_SHIFTNET_LOSS_ROBUST = 1 };
+typedef struct ves_shiftnet_config {
+    int dim;       /* matrix order n, 1..64 */
+    int n_params;  /* family parameters per matrix, 0..64 */
+    int hidden;    /* units per hidden layer: multiple of 16, 16..256; default 256 */
+    int layers;    /* hidden layers (tcgen05 BF16 GEMMs), 1..6; the output layer is FP32; default 3 */
+    int fourier;   /* extra features per parameter p: sin and cos of (pi/2) k p, k = 1..fourier
+                    * (n_params * fourier <= 64); default 0 */
+    int loss;      /* VES_SHIFTNET_LOSS_CHAMFER (squared distances, default) or _ROBUST
+                    * (sqrt(d^2 + delta^2) - delta per matched pair) */
+    float delta;   /* robust loss scale in standardised units; default 0.01 */
+    unsigned long long seed;  /* weight initialisation */
+} ves_shiftnet_config;
+void ves_shiftnet_default_config(ves_shiftnet_config *cfg);
+int ves_shiftnet_create_config(ves_shiftnet **net, const ves_shiftnet_config *cfg);
+/* the default configuration with the given order, parameter count, width and seed */
 int ves_shiftnet_create(ves_shiftnet **net, int dim, int n_params, int hidden, unsigned long long seed);
 void ves_shiftnet_destroy(ves_shiftnet *net);
 int ves_shiftnet_train(ves_shiftnet *net, long long count, int thread_cnt, const double *params,

@@ -80,3 +80,16 @@ def test_train_predict_checkpoint():
         rS2, iS2 = learned_shift.predict(net2, n, 4096, p, rA, iA)
         torch.cuda.synchronize()
         assert torch.equal(rS, rS2) and torch.equal(iS, iS2)
+
+
+def test_gate_closed_equals_plain_solver():
+    """With the gate closed (predictions never used) the shift-seeded solve is
+    the plain solver, bit for bit, and reports no fallbacks."""
+    import torch
+    n, N = 16, 4096
+    p, rA, iA = learned_shift.family(N, n, param_seed=12)
+    rE0, iE0, sw0 = learned_shift.solve_plain(n, N, rA, iA, TC, vectors=True)
+    far = torch.full_like(rE0, 100.0)
+    rE, iE, st, sw, fb, res = solve_shifts(n, N, rA, iA, far, torch.zeros_like(far), shift_gate=1e6)
+    assert torch.equal(rE, rE0) and torch.equal(iE, iE0) and torch.equal(sw, sw0)
+    assert fb.sum().item() == 0 and (st == 0).all()

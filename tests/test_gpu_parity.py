@@ -355,3 +355,26 @@ def test_device_stage_entry_points():
     ves.call_zunghr(n, bc, tc, hr, hi, t2r, t2i)
     torch.cuda.synchronize()
     np.testing.assert_array_equal(dr.cpu().numpy(), hr)
+
+
+def test_dropin_pipeline_chunks_equal_one_launch():
+    """The drop-in eigensolver() splits a large batch into chunks of SoA blocks
+    solved on two streams; its results equal one device launch bit for bit
+    (unequal chunks: 3 chunks of 141, 141 and 139 blocks)."""
+    import torch
+    import workloads
+    n, tc, bc = 4, 512, 421
+    N = bc * tc
+    rA, iA = workloads.gaussian_soa(N, n, seed=11, thread_cnt=tc)
+    dA = [torch.from_numpy(x).cuda() for x in (rA, iA)]
+    dE = [torch.empty(N * n, dtype=torch.float64, device="cuda") for _ in range(2)]
+    dV = [torch.empty_like(dA[0]) for _ in range(2)]
+    dT = [torch.empty_like(dA[0]) for _ in range(2)]
+    ves.eigensolve(n, bc, tc, dA[0], dA[1], dE[0], dE[1], dV[0], dV[1], rT=dT[0], iT=dT[1])
+    torch.cuda.synchronize()
+    hA = [rA.copy(), iA.copy()]
+    hE = [np.zeros(N * n) for _ in range(2)]
+    hV = [np.zeros_like(rA) for _ in range(2)]
+    ves.eigensolver(n, bc, tc, hA[0], hA[1], hE[0], hE[1], hV[0], hV[1])
+    for h, d in zip(hE + hV + hA, dE + dV + dT):
+        np.testing.assert_array_equal(h, d.cpu().numpy())

@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstdint>
 #include <cstring>
+#include <array>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -156,6 +157,32 @@ WsPlan workspace_plan(int precision, int n, long long N, bool vectors, int bps)
 // ---------------------------------------------------------------------------
 // Drop-in bodies (bool: success).
 // ---------------------------------------------------------------------------
+// Streams of the drop-in eigensolver's copy/solve pipeline, created once per
+// device (called with the pool mutex held).
+cudaStream_t pipeline_stream(int k)
+{
+    static std::vector<std::array<cudaStream_t, 2>> streams;  // [device][k]
+    int d = 0;
+    if (cudaGetDevice(&d) != cudaSuccess) return nullptr;
+    if ((int)streams.size() <= d) streams.resize(d + 1, std::array<cudaStream_t, 2>{nullptr, nullptr});
+    cudaStream_t &st = streams[d][k];
+    if (!st && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        st = nullptr;
+    }
+    return st;
+}
+
+// The reference's eigensolver() on host buffers.  Whole SoA blocks of
+// thread_cnt matrices are contiguous in every plane, so the batch is cut into
+// chunks of blocks and two streams alternate chunks: while one chunk is being
+// solved, the next one's input is copied in and the previous one's results are
+// copied out.  Each stream has its own workspace, since two solves can be
+// resident at once (which also fills the tail of each launch).  The issue
+// order (next chunk's copy-in and solve before this chunk's copy-out) keeps the
+// GPU busy even when the host buffers are pageable and copy-outs block the
+// calling thread.  Results are the same as one launch over the whole batch:
+// every matrix is solved by the same lane code whatever the grid.
 bool do_eigensolver(int dim, int bc, int tc, double *rA, double *iA, double *rE, double *iE, double *rV, double *iV)
 {
     ves::Geom g;
@@ -167,23 +194,64 @@ bool do_eigensolver(int dim, int bc, int tc, double *rA, double *iA, double *rE,
     double *dAr = b.d(0, nm), *dAi = b.d(1, nm), *dVr = b.d(2, nm), *dVi = b.d(3, nm);
     double *dEr = b.d(4, nv), *dEi = b.d(5, nv);
     NEED(dAr); NEED(dAi); NEED(dVr); NEED(dVi); NEED(dEr); NEED(dEi);
-    const size_t wsb = ves::fused_workspace_bytes(dim, g.N, 0, nullptr, nullptr);
-    void *ws = b.raw(6, wsb);
-    NEED(ws);
-    if (!h2d(dAr, rA, nm * 8) || !h2d(dAi, iA, nm * 8)) return false;
-    ves::FusedArgs a{};
-    a.g = g;
-    a.rA = dAr; a.iA = dAi;
-    a.rE = dEr; a.iE = dEi;
-    a.rV = dVr; a.iV = dVi;
-    a.rT = dAr; a.iT = dAi;  // A is overwritten with T, as in the reference
-    a.ws = ws;
-    a.max_its = 30;
-    a.vnorm = VES_VNORM_REFERENCE;
-    if (!cuda_ok(ves::launch_fused_fp64(a, 0), "eigensolver kernel launch")) return false;
-    if (!sync_ok("eigensolver kernel")) return false;
-    return d2h(rA, dAr, nm * 8) && d2h(iA, dAi, nm * 8) && d2h(rE, dEr, nv * 8) && d2h(iE, dEi, nv * 8) &&
-           d2h(rV, dVr, nm * 8) && d2h(iV, dVi, nm * 8);
+
+    constexpr long long kMinChunk = 65536;  // matrices per chunk: keeps each launch's persistent grid busy
+    constexpr long long kMaxChunks = 8;
+    long long nchunks = std::min<long long>(kMaxChunks, std::max<long long>(1, g.N / kMinChunk));
+    nchunks = std::min<long long>(nchunks, bc);
+    const long long cb = (bc + nchunks - 1) / nchunks;  // blocks per chunk
+    nchunks = (bc + cb - 1) / cb;
+    const size_t wsb = ves::fused_workspace_bytes(dim, cb * (long long)tc, 0, nullptr, nullptr);
+    void *ws[2] = {b.raw(6, wsb), nchunks > 1 ? b.raw(9, wsb) : nullptr};
+    NEED(ws[0]);
+    if (nchunks > 1) NEED(ws[1]);
+    cudaStream_t st[2] = {pipeline_stream(0), pipeline_stream(1)};
+    if (!st[0] || !st[1]) { set_error("stream creation failed"); return false; }
+
+    const size_t mstride = (size_t)tc * dim * dim, vstride = (size_t)tc * dim;  // elements per block
+    auto chunk = [&](long long c, long long &b0, long long &nb) {
+        b0 = c * cb;
+        nb = std::min<long long>(cb, bc - b0);
+    };
+    auto copy_in_and_solve = [&](long long c) -> bool {
+        long long b0, nb;
+        chunk(c, b0, nb);
+        cudaStream_t s = st[c & 1];
+        const size_t mo = b0 * mstride, vo = b0 * vstride, mb = nb * mstride * 8;
+        if (!cuda_ok(cudaMemcpyAsync(dAr + mo, rA + mo, mb, cudaMemcpyHostToDevice, s), "H2D") ||
+            !cuda_ok(cudaMemcpyAsync(dAi + mo, iA + mo, mb, cudaMemcpyHostToDevice, s), "H2D"))
+            return false;
+        ves::FusedArgs a{};
+        a.g = ves::Geom{dim, nb * (long long)tc, tc};
+        a.rA = dAr + mo; a.iA = dAi + mo;
+        a.rE = dEr + vo; a.iE = dEi + vo;
+        a.rV = dVr + mo; a.iV = dVi + mo;
+        a.rT = dAr + mo; a.iT = dAi + mo;  // A is overwritten with T, as in the reference
+        a.ws = ws[c & 1];
+        a.max_its = 30;
+        a.vnorm = VES_VNORM_REFERENCE;
+        return cuda_ok(ves::launch_fused_fp64(a, s), "eigensolver kernel launch");
+    };
+    auto copy_out = [&](long long c) -> bool {
+        long long b0, nb;
+        chunk(c, b0, nb);
+        cudaStream_t s = st[c & 1];
+        const size_t mo = b0 * mstride, vo = b0 * vstride, mb = nb * mstride * 8, vb = nb * vstride * 8;
+        return cuda_ok(cudaMemcpyAsync(rE + vo, dEr + vo, vb, cudaMemcpyDeviceToHost, s), "D2H") &&
+               cuda_ok(cudaMemcpyAsync(iE + vo, dEi + vo, vb, cudaMemcpyDeviceToHost, s), "D2H") &&
+               cuda_ok(cudaMemcpyAsync(rV + mo, dVr + mo, mb, cudaMemcpyDeviceToHost, s), "D2H") &&
+               cuda_ok(cudaMemcpyAsync(iV + mo, dVi + mo, mb, cudaMemcpyDeviceToHost, s), "D2H") &&
+               cuda_ok(cudaMemcpyAsync(rA + mo, dAr + mo, mb, cudaMemcpyDeviceToHost, s), "D2H") &&
+               cuda_ok(cudaMemcpyAsync(iA + mo, dAi + mo, mb, cudaMemcpyDeviceToHost, s), "D2H");
+    };
+    bool ok = copy_in_and_solve(0);
+    for (long long c = 0; ok && c < nchunks; ++c) {
+        if (c + 1 < nchunks) ok = copy_in_and_solve(c + 1);
+        ok = ok && copy_out(c);
+    }
+    const bool s0 = cuda_ok(cudaStreamSynchronize(st[0]), "eigensolver stream 0");
+    const bool s1 = cuda_ok(cudaStreamSynchronize(st[1]), "eigensolver stream 1");
+    return ok && s0 && s1;
 }
 
 bool do_hessenberg(int dim, int bc, int tc, double *rA, double *iA, double *rQ, double *iQ)
@@ -423,6 +491,7 @@ void ves_default_options(ves_options *opt)
     opt->blocks_per_sm = 0;
     opt->varsize_order = 0;
     opt->shift_sweeps = 1;
+    opt->shift_gate = 0.f;
 }
 
 size_t ves_eigensolve_workspace_size(int dim, int block_cnt, int thread_cnt, const ves_options *opt)
@@ -621,7 +690,8 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *
     ves_default_options(&o);
     if (opt) o = *opt;
     if (o.max_its < 0 || o.max_its > 10000 || o.vnorm < 0 || o.vnorm > 2 || o.shift_sweeps < 0 ||
-        o.shift_sweeps > 9 || o.blocks_per_sm < 0 || o.blocks_per_sm > 16) {
+        o.shift_sweeps > 9 || o.blocks_per_sm < 0 || o.blocks_per_sm > 16 || !(o.shift_gate >= 0.f) ||
+        o.shift_gate > 1e6f) {
         set_error("option out of range");
         return VES_ERR_ARG;
     }
@@ -645,6 +715,7 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *
     a.vnorm = o.vnorm;
     a.rS = rS; a.iS = iS;
     a.shift_sweeps = o.shift_sweeps;
+    a.shift_gate = o.shift_gate;
     a.fallbacks = fallbacks;
     a.blocks_per_sm = o.blocks_per_sm;
     return native(cuda_ok(ves::launch_fused_fp64(a, (cudaStream_t)stream), "learned-shift solve launch"));

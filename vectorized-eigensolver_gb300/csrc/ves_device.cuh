@@ -416,34 +416,44 @@ __device__ __forceinline__ void zlarfg2(cx<R> &v0, cx<R> &v1, cx<R> &t1)
 // the reference's shifts take over.  An eigenvalue that still needs more than
 // sweeps + 2 sweeps counts as a fallback to Wilkinson.
 struct NoShiftPredictions {
-    template <class R> __device__ __forceinline__ void pick(int, int, cx<R> &) {}
+    template <class R> __device__ __forceinline__ void pick(int, int, cx<R> &, R) {}
     __device__ __forceinline__ void deflated(int) {}
 };
+// Learned shifts: for the first `sweeps` sweeps of an eigenvalue, the QR shift
+// is the unused prediction nearest to the Wilkinson estimate -- provided the
+// subdiagonal |H(I,I-1)| still exceeds `gate` (absolute) when the eigenvalue
+// starts: once it is that small the Wilkinson shift is already more accurate
+// than the predictions, and they are left alone.
 struct ShiftPredictions {
     const double *re, *im;  // this matrix's predictions, stride s
     long long s;
     int n, sweeps;
+    double gate;
     unsigned long long used;
     int current;
     int fallbacks;
-    template <class R> __device__ __forceinline__ void pick(int its, int, cx<R> &t)
+    template <class R> __device__ __forceinline__ void pick(int its, int, cx<R> &t, R hsub)
     {
-        if (its >= sweeps || its == 10 || its == 20) return;
         if (its == 0) {
-            R best = R(0);
-            int bi = -1;
-            for (int k = 0; k < n; ++k) {
-                if ((used >> k) & 1ULL) continue;
-                const R dr = (R)re[k * s] - t.r, di = (R)im[k * s] - t.i;
-                const R d = dr * dr + di * di;
-                if (bi < 0 || d < best) { best = d; bi = k; }
+            current = -1;
+            if (sweeps > 0 && hsub > (R)gate) {
+                R best = R(0);
+                int bi = -1;
+                for (int k = 0; k < n; ++k) {
+                    if ((used >> k) & 1ULL) continue;
+                    const R dr = (R)re[k * s] - t.r, di = (R)im[k * s] - t.i;
+                    const R d = dr * dr + di * di;
+                    if (bi < 0 || d < best) { best = d; bi = k; }
+                }
+                current = bi;
+                if (bi >= 0) used |= 1ULL << bi;
             }
-            current = bi;
-            if (bi >= 0) used |= 1ULL << bi;
         }
+        if (its >= sweeps || its == 10 || its == 20) return;
         if (current >= 0) t = mk((R)re[current * s], (R)im[current * s]);
     }
-    __device__ __forceinline__ void deflated(int its) { if (its > sweeps + 2) ++fallbacks; }
+    // a predicted eigenvalue that still needed more than sweeps + 2 sweeps
+    __device__ __forceinline__ void deflated(int its) { if (current >= 0 && its > sweeps + 2) ++fallbacks; }
 };
 
 template <class R, bool kSchur = true, class MH, class MZ, class SP = NoShiftPredictions>
@@ -473,7 +483,7 @@ __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool va
                     continue;
                 }
                 cx<R> t = qr_shift<R>(I, L, its, H);
-                if (sp) sp->template pick<R>(its, I, t);
+                if (sp) sp->template pick<R>(its, I, t, fabs(H.ld(I, I - 1).r));
                 const cx<R> h11s = csub(H.ld(L, L), t);
                 const R h21 = H.ld(L + 1, L).r;
                 const R rs = R(1) / (cabs1(h11s) + fabs(h21));

@@ -35,6 +35,7 @@ struct FusedArgs {
     // counts per matrix the eigenvalues that still needed Wilkinson's shift
     const double *rS, *iS;
     int shift_sweeps;
+    float shift_gate;  // predictions used only while |H(I,I-1)| > shift_gate * ||A||_F / sqrt(n)
     int *fallbacks;
     int blocks_per_sm;  // persistent grid: blocks (4 warps) per SM; 0 = default
 };

@@ -79,6 +79,7 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
         const long long mo = valid ? soa_mat_off(m, n, tc) : 0;
         const long long vo = valid ? soa_vec_off(m, n, tc) : 0;
         int status = 0, sweeps = 0;
+        double fro2 = 0.0;  // ||A||_F^2: scale of the learned-shift gate
 
         if (valid) {
             const MatSoA<double> A{const_cast<double *>(a.rA) + mo, const_cast<double *>(a.iA) + mo, tc, n};
@@ -87,6 +88,7 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
                 for (int i = 1; i <= n; ++i) {
                     const cx<double> v = A.ld(i, j);
                     bad |= nonfinite(v.r) | nonfinite(v.i);
+                    if (kLearned) fro2 = fma(v.i, v.i, fma(v.r, v.r, fro2));
                     H.st(i, j, v);
                 }
             if (bad) status |= ST_NONFINITE;
@@ -101,6 +103,7 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
             sp.s = tc;
             sp.n = n;
             sp.sweeps = a.shift_sweeps;
+            sp.gate = (double)a.shift_gate * sqrt(fro2 / (double)n);
             sp.used = 0;
             sp.current = -1;
             sp.fallbacks = 0;

@@ -8,10 +8,17 @@
 //             Kin (a multiple of 32), BF16
 //   network   Kin -> H -> H -> H -> Nout, GELU after the hidden layers,
 //             BF16 weights and activations, FP32 accumulation (in TMEM)
-//   targets   the eigenvalues the plain solver computed, sorted by real part
-//             (a canonical order, so the loss is a plain MSE), as
-//             [Re (n), Im (n)], standardised, zero-padded to Nout (multiple of 16)
-//   training  mean-squared error, backward pass and Adam in FP32 on CUDA cores
+//   targets   the eigenvalues the plain solver computed, as [Re (n), Im (n)]
+//             (sorted by real part, which only seeds the output order), shifted
+//             by the mean real / imaginary part and divided by one common
+//             standard deviation, zero-padded to Nout (multiple of 16)
+//   training  the loss is the symmetric Chamfer distance between the predicted
+//             set and the eigenvalue set, (1/2n) [sum_i min_j |y_i - l_j|^2 +
+//             sum_j min_i |y_i - l_j|^2]: an eigenvalue set has no canonical
+//             order that is continuous in the matrix (any order by real part
+//             jumps where two real parts cross), and the solver only needs
+//             every eigenvalue to have a prediction nearby.  Backward pass and
+//             Adam (cosine learning-rate decay to 1/50) in FP32 on CUDA cores
 //             (the batch GEMMs of the backward pass are a few MFLOP)
 //   inference one forward pass per matrix, denormalised to n complex shifts
 #include "ves.h"
@@ -51,6 +58,7 @@ cudaError_t launch_gemm_bf16(int M, int N, int K, const void *A, int lda, const 
 namespace {
 
 constexpr int kMaxDimNet = 64;
+constexpr int kMaxLayers = 6;  // hidden layers
 typedef __nv_bfloat16 bf16;
 
 __device__ __forceinline__ long long soa_off_s(long long m, long long len, int tc)
@@ -58,29 +66,43 @@ __device__ __forceinline__ long long soa_off_s(long long m, long long len, int t
     return (m / tc) * (long long)tc * len + (m % tc);
 }
 
-// raw (unnormalised) features of matrix m into f[0..P+2n)
-__device__ __forceinline__ void raw_features(long long m, int n, int P, int tc, const double *params, const double *rA,
-                                             const double *iA, float *f)
+constexpr int kMaxFourier = 64;  // n_params * fourier
+constexpr int kMaxFeat = 64 + 2 * kMaxFourier + 2 * kMaxDimNet;
+
+// raw (unnormalised) features of matrix m into f[0 .. P + 2PF + 2n):
+// parameters, sin / cos ((pi/2) k p) for k = 1..F, Re diag A, Im diag A
+__device__ __forceinline__ void raw_features(long long m, int n, int P, int F, int tc, const double *params,
+                                             const double *rA, const double *iA, float *f)
 {
-    for (int p = 0; p < P; ++p) f[p] = params ? (float)params[m * P + p] : 0.f;
+    for (int q = 0; q < P; ++q) {
+        const float x = params ? (float)params[m * P + q] : 0.f;
+        f[q] = x;
+        for (int k = 1; k <= F; ++k) {
+            float sn, cs;
+            sincospif(0.5f * (float)k * x, &sn, &cs);
+            f[P + 2 * (q * F + k - 1)] = sn;
+            f[P + 2 * (q * F + k - 1) + 1] = cs;
+        }
+    }
+    const int o = P + 2 * P * F;
     const long long mo = soa_off_s(m, (long long)n * n, tc);
     for (int i = 0; i < n; ++i) {
         const long long k = mo + (long long)(i + i * n) * tc;
-        f[P + i] = (float)rA[k];
-        f[P + n + i] = (float)iA[k];
+        f[o + i] = (float)rA[k];
+        f[o + n + i] = (float)iA[k];
     }
 }
 
 // features -> standardised BF16 rows [count x kin_pad]
-__global__ void features_kernel(long long count, int n, int P, int tc, const double *params, const double *rA,
+__global__ void features_kernel(long long count, int n, int P, int F, int tc, const double *params, const double *rA,
                                 const double *iA, const float *mean, const float *stdv, int kin, int kin_pad, bf16 *X,
                                 const int *rows)
 {
     const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= count) return;
     const long long m = rows ? rows[r] : r;
-    float f[3 * kMaxDimNet];
-    raw_features(m, n, P, tc, params, rA, iA, f);
+    float f[kMaxFeat];
+    raw_features(m, n, P, F, tc, params, rA, iA, f);
     for (int c = 0; c < kin_pad; ++c) {
         float v = 0.f;
         if (c < kin) v = mean ? (f[c] - mean[c]) / stdv[c] : f[c];
@@ -125,24 +147,7 @@ __global__ void targets_kernel(long long count, int n, int tc, const double *rE,
     for (int c = 0; c < nout_pad; ++c) T[r * nout_pad + c] = c < 2 * n ? (mean ? (t[c] - mean[c]) / stdv[c] : t[c]) : 0.f;
 }
 
-// column mean and standard deviation of an FP32 (count x cols) table, or of
-// the BF16 feature table, one thread per column
-__global__ void colstats_f32_kernel(long long count, int cols, int ld, const float *T, float *mean, float *stdv)
-{
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= cols) return;
-    double s = 0.0, s2 = 0.0;
-    for (long long r = 0; r < count; ++r) {
-        const double v = T[r * ld + c];
-        s += v;
-        s2 += v * v;
-    }
-    const double mu = s / (double)count;
-    const double var = s2 / (double)count - mu * mu;
-    mean[c] = (float)mu;
-    stdv[c] = (float)(var > 1e-12 ? sqrt(var) : 1.0);
-}
-
+// column mean and standard deviation of the BF16 feature table, one thread per column
 __global__ void colstats_bf16_kernel(long long count, int cols, int ld, const bf16 *X, float *mean, float *stdv)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -159,20 +164,109 @@ __global__ void colstats_bf16_kernel(long long count, int cols, int ld, const bf
     stdv[c] = (float)(var > 1e-12 ? sqrt(var) : 1.0);
 }
 
-// ---- training kernels (FP32, CUDA cores) -----------------------------------
-// loss and dY = 2 (Y - T) / (B * nvalid) on the valid columns
-__global__ void mse_kernel(int B, int ncols, int nvalid, const float *Y, const float *T, float *dY, float *loss)
+// Target normalisation: mean of the real parts, mean of the imaginary parts,
+// one common standard deviation (distances stay isotropic in the complex
+// plane).  One block; T holds raw targets [count x ld].
+__global__ void target_stats_kernel(long long count, int n, int ld, int nout_pad, const float *T, float *mean,
+                                    float *stdv)
 {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double red[4][256];
+    double sr = 0.0, si = 0.0, sr2 = 0.0, si2 = 0.0;
+    const long long total = count * n;
+    for (long long e = threadIdx.x; e < total; e += blockDim.x) {
+        const long long r = e / n;
+        const int i = (int)(e % n);
+        const double vr = T[r * ld + i], vi = T[r * ld + n + i];
+        sr += vr;
+        sr2 += vr * vr;
+        si += vi;
+        si2 += vi * vi;
+    }
+    red[0][threadIdx.x] = sr;
+    red[1][threadIdx.x] = si;
+    red[2][threadIdx.x] = sr2;
+    red[3][threadIdx.x] = si2;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h)
+            for (int k = 0; k < 4; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double c = (double)total;
+        const double mr = red[0][0] / c, mi = red[1][0] / c;
+        const double var = 0.5 * ((red[2][0] / c - mr * mr) + (red[3][0] / c - mi * mi));
+        const float sd = (float)(var > 1e-24 ? sqrt(var) : 1.0);
+        for (int k = 0; k < nout_pad; ++k) {
+            mean[k] = k < n ? (float)mr : (k < 2 * n ? (float)mi : 0.f);
+            stdv[k] = k < 2 * n ? sd : 1.f;
+        }
+    }
+}
+
+// ---- training kernels (FP32, CUDA cores) -----------------------------------
+// Symmetric Chamfer loss between the predicted set y and the eigenvalue set t
+// of each sample (rows of Y, T: [Re (n), Im (n), padding]) and its gradient
+// dY; one thread per sample.  Every prediction is matched to its nearest
+// eigenvalue and every eigenvalue to its nearest prediction; a matched pair at
+// squared distance d2 costs d2 (kind 0) or sqrt(d2 + delta^2) - delta (kind 1,
+// robust: the rare far pairs near colliding eigenvalues do not dominate).
+// loss += batch mean of (1/2n) sum of the costs.
+__device__ __forceinline__ float pair_cost(int kind, float d2, float delta, float &gscale)
+{
+    if (kind == 0) { gscale = 2.f; return d2; }
+    const float r = sqrtf(d2 + delta * delta);
+    gscale = 1.f / r;
+    return r - delta;
+}
+
+__global__ void chamfer_kernel(int B, int n, int ld, const float *Y, const float *T, float *dY, float *loss, int kind,
+                               float delta)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
     float l = 0.f;
-    if (i < (long long)B * ncols) {
-        const int c = (int)(i % ncols);
-        const float d = c < nvalid ? Y[i] - T[i] : 0.f;
-        dY[i] = 2.f * d / ((float)B * nvalid);
-        l = d * d;
+    if (b < B) {
+        float yr[kMaxDimNet], yi[kMaxDimNet], tr[kMaxDimNet], ti[kMaxDimNet], gr[kMaxDimNet], gi[kMaxDimNet];
+        const float *y = Y + (long long)b * ld, *t = T + (long long)b * ld;
+        for (int i = 0; i < n; ++i) {
+            yr[i] = y[i]; yi[i] = y[n + i];
+            tr[i] = t[i]; ti[i] = t[n + i];
+            gr[i] = 0.f; gi[i] = 0.f;
+        }
+        const float w = 1.f / (2.f * (float)n * (float)B);
+        for (int i = 0; i < n; ++i) {  // each prediction to its nearest eigenvalue
+            float best = 0.f;
+            int bj = -1;
+            for (int j = 0; j < n; ++j) {
+                const float dr = yr[i] - tr[j], di = yi[i] - ti[j];
+                const float d = dr * dr + di * di;
+                if (bj < 0 || d < best) { best = d; bj = j; }
+            }
+            float gs;
+            l += pair_cost(kind, best, delta, gs);
+            gr[i] += gs * w * (yr[i] - tr[bj]);
+            gi[i] += gs * w * (yi[i] - ti[bj]);
+        }
+        for (int j = 0; j < n; ++j) {  // each eigenvalue to its nearest prediction
+            float best = 0.f;
+            int bi = -1;
+            for (int i = 0; i < n; ++i) {
+                const float dr = yr[i] - tr[j], di = yi[i] - ti[j];
+                const float d = dr * dr + di * di;
+                if (bi < 0 || d < best) { best = d; bi = i; }
+            }
+            float gs;
+            l += pair_cost(kind, best, delta, gs);
+            gr[bi] += gs * w * (yr[bi] - tr[j]);
+            gi[bi] += gs * w * (yi[bi] - ti[j]);
+        }
+        float *g = dY + (long long)b * ld;
+        for (int i = 0; i < n; ++i) { g[i] = gr[i]; g[n + i] = gi[i]; }
+        for (int c = 2 * n; c < ld; ++c) g[c] = 0.f;
+        l *= w;
     }
     for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(FULL, l, o);
-    if ((threadIdx.x & 31) == 0 && l != 0.f) atomicAdd(loss, l / ((float)B * nvalid));
+    if ((threadIdx.x & 31) == 0 && l != 0.f) atomicAdd(loss, l);
 }
 
 __device__ __forceinline__ float gelu_grad(float x)
@@ -190,19 +284,44 @@ __global__ void gelu_bwd_kernel(long long total, const float *dH, const float *Z
     if (i < total) dZ[i] = dH[i] * gelu_grad(Z[i]);
 }
 
+__device__ __forceinline__ float to_f32(bf16 x) { return __bfloat162float(x); }
+__device__ __forceinline__ float to_f32(float x) { return x; }
+
 // dW[o][i] = sum_b dZ[b][o] * H[b][i];  db[o] = sum_b dZ[b][o] (column i == 0 thread)
-__global__ void dw_kernel(int B, int out, int in, const float *dZ, const bf16 *H, int ldh, float *dW, float *db)
+template <class HT>
+__global__ void dw_kernel(int B, int out, int in, const float *dZ, const HT *H, int ldh, float *dW, float *db)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, o = blockIdx.y;
     if (o >= out) return;
     float acc = 0.f, accb = 0.f;
     for (int b = 0; b < B; ++b) {
         const float g = dZ[(long long)b * out + o];
-        if (i < in) acc = fmaf(g, __bfloat162float(H[(long long)b * ldh + i]), acc);
+        if (i < in) acc = fmaf(g, to_f32(H[(long long)b * ldh + i]), acc);
         accb += g;
     }
     if (i < in) dW[(long long)o * in + i] = acc;
     if (i == 0) db[o] = accb;
+}
+
+// FP32 activations of the last hidden layer: Hf = GELU(Z)
+__global__ void gelu_f32_kernel(long long total, const float *Z, float *Hf)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < total) Hf[i] = tc::gelu(Z[i]);
+}
+
+// Output layer in FP32 on CUDA cores (no BF16 rounding of the last hidden
+// activations or of the output weights): Y[r][o] = b[o] + sum_i W[o][i] Hf[r][i],
+// one thread per (r, o).
+__global__ void dense_out_kernel(int rows, int out, int in, const float *Hf, const float *W, const float *b, float *Y)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)rows * out) return;
+    const int r = (int)(t / out), o = (int)(t % out);
+    const float *h = Hf + (long long)r * in, *w = W + (long long)o * in;
+    float acc = b[o];
+    for (int i = 0; i < in; ++i) acc = fmaf(w[i], h[i], acc);
+    Y[t] = acc;
 }
 
 // dH[b][i] = sum_o dZ[b][o] * W[o][i]
@@ -259,10 +378,15 @@ inline unsigned nb(long long n, int t = 256) { return (unsigned)((n + t - 1) / t
 // The network object and its C ABI.
 // ---------------------------------------------------------------------------
 struct ves_shiftnet {
-    int n = 0, P = 0, H = 0, kin = 0, kin_pad = 0, nout = 0, nout_pad = 0;
-    int in[4] = {}, out[4] = {};
-    float *W[4] = {}, *b[4] = {}, *mW[4] = {}, *vW[4] = {}, *mb[4] = {}, *vb[4] = {};
-    ves::bf16 *Wb[4] = {};
+    ves_shiftnet_config cfg{};
+    int n = 0, P = 0, H = 0, L = 0, F = 0, kin = 0, kin_pad = 0, nout = 0, nout_pad = 0;
+    // layers 0..L-1: hidden (tcgen05, BF16 in, FP32 accumulate, GELU);
+    // layer L: output (FP32, CUDA cores)
+    int in[ves::kMaxLayers + 1] = {}, out[ves::kMaxLayers + 1] = {};
+    float *W[ves::kMaxLayers + 1] = {}, *b[ves::kMaxLayers + 1] = {};
+    float *mW[ves::kMaxLayers + 1] = {}, *vW[ves::kMaxLayers + 1] = {};
+    float *mb[ves::kMaxLayers + 1] = {}, *vb[ves::kMaxLayers + 1] = {};
+    ves::bf16 *Wb[ves::kMaxLayers] = {};
     float *fmean = nullptr, *fstd = nullptr, *tmean = nullptr, *tstd = nullptr;
     long long step = 0;
     int dev = 0;
@@ -272,9 +396,10 @@ namespace {
 
 void net_free(ves_shiftnet *t)
 {
-    for (int l = 0; l < 4; ++l) {
+    for (int l = 0; l <= t->L; ++l) {
         cudaFree(t->W[l]); cudaFree(t->b[l]); cudaFree(t->mW[l]); cudaFree(t->vW[l]);
-        cudaFree(t->mb[l]); cudaFree(t->vb[l]); cudaFree(t->Wb[l]);
+        cudaFree(t->mb[l]); cudaFree(t->vb[l]);
+        if (l < t->L) cudaFree(t->Wb[l]);
     }
     cudaFree(t->fmean); cudaFree(t->fstd); cudaFree(t->tmean); cudaFree(t->tstd);
 }
@@ -282,7 +407,7 @@ void net_free(ves_shiftnet *t)
 bool net_alloc(ves_shiftnet *t)
 {
     bool ok = true;
-    for (int l = 0; l < 4; ++l) {
+    for (int l = 0; l <= t->L && ok; ++l) {
         const size_t nw = (size_t)t->out[l] * t->in[l];
         ok &= cudaMalloc(&t->W[l], nw * 4) == cudaSuccess;
         ok &= cudaMalloc(&t->b[l], t->out[l] * 4) == cudaSuccess;
@@ -290,7 +415,7 @@ bool net_alloc(ves_shiftnet *t)
         ok &= cudaMalloc(&t->vW[l], nw * 4) == cudaSuccess;
         ok &= cudaMalloc(&t->mb[l], t->out[l] * 4) == cudaSuccess;
         ok &= cudaMalloc(&t->vb[l], t->out[l] * 4) == cudaSuccess;
-        ok &= cudaMalloc(&t->Wb[l], nw * 2) == cudaSuccess;
+        if (l < t->L) ok &= cudaMalloc(&t->Wb[l], nw * 2) == cudaSuccess;
         if (!ok) break;
         cudaMemset(t->mW[l], 0, nw * 4);
         cudaMemset(t->vW[l], 0, nw * 4);
@@ -302,63 +427,96 @@ bool net_alloc(ves_shiftnet *t)
     return ok;
 }
 
-void set_geometry(ves_shiftnet *t, int n, int P, int H)
+bool config_ok(const ves_shiftnet_config &c)
 {
-    t->n = n; t->P = P; t->H = H;
-    t->kin = P + 2 * n;
-    t->kin_pad = (t->kin + 31) / 32 * 32;
-    t->nout = 2 * n;
-    t->nout_pad = (t->nout + 15) / 16 * 16;
-    const int ins[4] = {t->kin_pad, H, H, H}, outs[4] = {H, H, H, t->nout_pad};
-    for (int l = 0; l < 4; ++l) { t->in[l] = ins[l]; t->out[l] = outs[l]; }
+    return c.dim >= 1 && c.dim <= ves::kMaxDimNet && c.n_params >= 0 && c.n_params <= 64 && c.hidden >= 16 &&
+           c.hidden <= 256 && (c.hidden % 16) == 0 && c.layers >= 1 && c.layers <= ves::kMaxLayers &&
+           c.fourier >= 0 && c.n_params * c.fourier <= ves::kMaxFourier && (c.loss == 0 || c.loss == 1) &&
+           c.delta > 0.f && c.delta < 1e3f;
 }
 
-// forward over `rows` rows of X (BF16 [rows x kin_pad]); Z[l] FP32 pre-activations,
-// Hs[l] BF16 activations ([rows x H]); Y = Z[3] [rows x nout_pad]
-cudaError_t forward(const ves_shiftnet *t, int rows, const ves::bf16 *X, float *const Z[4], ves::bf16 *const Hs[3],
-                    int *err, cudaStream_t st)
+void set_geometry(ves_shiftnet *t, const ves_shiftnet_config &c)
+{
+    t->cfg = c;
+    t->n = c.dim; t->P = c.n_params; t->H = c.hidden; t->L = c.layers; t->F = c.fourier;
+    t->kin = t->P + 2 * t->P * t->F + 2 * t->n;
+    t->kin_pad = (t->kin + 31) / 32 * 32;
+    t->nout = 2 * t->n;
+    t->nout_pad = (t->nout + 15) / 16 * 16;
+    for (int l = 0; l <= t->L; ++l) {
+        t->in[l] = l == 0 ? t->kin_pad : t->H;
+        t->out[l] = l == t->L ? t->nout_pad : t->H;
+    }
+}
+
+// Activation buffers of a forward pass over `rows` rows.
+struct Acts {
+    float *Z[ves::kMaxLayers] = {};     // FP32 pre-activations of the hidden layers [rows x H]
+    ves::bf16 *Hs[ves::kMaxLayers] = {};  // BF16 activations of the hidden layers [rows x H]
+    float *Hf = nullptr;                  // FP32 activations of the last hidden layer
+    float *Y = nullptr;                   // output [rows x nout_pad]
+};
+
+size_t acts_bytes(const ves_shiftnet *t, size_t rows)
+{
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    return t->L * (al(rows * t->H * 4) + al(rows * t->H * 2)) + al(rows * t->H * 4) + al(rows * t->nout_pad * 4);
+}
+
+Acts carve_acts(const ves_shiftnet *t, size_t rows, char *&w)
+{
+    auto take = [&](size_t bytes) { char *p = w; w += (bytes + 255) & ~(size_t)255; return p; };
+    Acts a;
+    for (int l = 0; l < t->L; ++l) {
+        a.Z[l] = reinterpret_cast<float *>(take(rows * t->H * 4));
+        a.Hs[l] = reinterpret_cast<ves::bf16 *>(take(rows * t->H * 2));
+    }
+    a.Hf = reinterpret_cast<float *>(take(rows * t->H * 4));
+    a.Y = reinterpret_cast<float *>(take(rows * t->nout_pad * 4));
+    return a;
+}
+
+// forward over `rows` rows of X (BF16 [rows x kin_pad])
+cudaError_t forward(const ves_shiftnet *t, int rows, const ves::bf16 *X, const Acts &a, int *err, cudaStream_t st)
 {
     const void *in = X;
     int ld = t->kin_pad;
-    for (int l = 0; l < 4; ++l) {
-        const bool last = l == 3;
-        cudaError_t e = ves::launch_gemm_bf16(rows, t->out[l], t->in[l], in, ld, t->Wb[l], t->in[l], t->b[l],
-                                              last ? 0 : 1, last ? nullptr : Hs[l], Z[l], t->out[l], err, st);
+    for (int l = 0; l < t->L; ++l) {
+        cudaError_t e = ves::launch_gemm_bf16(rows, t->H, t->in[l], in, ld, t->Wb[l], t->in[l], t->b[l], 1, a.Hs[l],
+                                              a.Z[l], t->H, err, st);
         if (e != cudaSuccess) return e;
-        if (!last) { in = Hs[l]; ld = t->out[l]; }
+        in = a.Hs[l];
+        ld = t->H;
     }
-    return cudaSuccess;
+    const long long nh = (long long)rows * t->H;
+    ves::gelu_f32_kernel<<<ves::nb(nh), 256, 0, st>>>(nh, a.Z[t->L - 1], a.Hf);
+    const long long no = (long long)rows * t->nout_pad;
+    ves::dense_out_kernel<<<ves::nb(no), 256, 0, st>>>(rows, t->nout_pad, t->H, a.Hf, t->W[t->L], t->b[t->L], a.Y);
+    return cudaGetLastError();
 }
 
-
-}  // namespace
-
-extern "C" {
-
-int ves_shiftnet_create(ves_shiftnet **out, int dim, int n_params, int hidden, unsigned long long seed)
+int create_from_config(ves_shiftnet **out, const ves_shiftnet_config &c)
 {
-    if (!out || dim < 1 || dim > ves::kMaxDimNet || n_params < 0 || n_params > 64 || hidden < 16 || hidden > 256 ||
-        (hidden % 16))
-        return VES_ERR_ARG;
+    if (!out || !config_ok(c)) return VES_ERR_ARG;
     ves_shiftnet *t = new ves_shiftnet();
     cudaGetDevice(&t->dev);
-    set_geometry(t, dim, n_params, hidden);
+    set_geometry(t, c);
     if (!net_alloc(t)) { net_free(t); delete t; return VES_ERR_NOMEM; }
     // He-style initialisation from a fixed seed (host), zero biases, identity normalisation
-    std::mt19937_64 rng(seed);
+    std::mt19937_64 rng(c.seed);
     std::normal_distribution<float> nd(0.f, 1.f);
-    for (int l = 0; l < 4; ++l) {
+    for (int l = 0; l <= t->L; ++l) {
         const int fan_in = l == 0 ? t->kin : t->in[l];
         std::vector<float> w((size_t)t->out[l] * t->in[l], 0.f);
-        const float sc = std::sqrt(2.f / (float)fan_in);
+        const float sc = std::sqrt((l == t->L ? 1.f : 2.f) / (float)fan_in);
         for (int o = 0; o < t->out[l]; ++o)
             for (int i = 0; i < t->in[l]; ++i)
-                if ((l != 0 || i < t->kin) && (l != 3 || o < t->nout)) w[(size_t)o * t->in[l] + i] = nd(rng) * sc;
+                if ((l != 0 || i < t->kin) && (l != t->L || o < t->nout)) w[(size_t)o * t->in[l] + i] = nd(rng) * sc;
         cudaMemcpy(t->W[l], w.data(), w.size() * 4, cudaMemcpyHostToDevice);
         cudaMemset(t->b[l], 0, t->out[l] * 4);
-        ves::to_bf16_kernel<<<ves::nb((long long)w.size()), 256>>>((long long)w.size(), t->W[l], t->Wb[l]);
+        if (l < t->L) ves::to_bf16_kernel<<<ves::nb((long long)w.size()), 256>>>((long long)w.size(), t->W[l], t->Wb[l]);
     }
-    std::vector<float> zero(256, 0.f), one(256, 1.f);
+    std::vector<float> zero(512, 0.f), one(512, 1.f);
     cudaMemcpy(t->fmean, zero.data(), t->kin_pad * 4, cudaMemcpyHostToDevice);
     cudaMemcpy(t->fstd, one.data(), t->kin_pad * 4, cudaMemcpyHostToDevice);
     cudaMemcpy(t->tmean, zero.data(), t->nout_pad * 4, cudaMemcpyHostToDevice);
@@ -366,6 +524,40 @@ int ves_shiftnet_create(ves_shiftnet **out, int dim, int n_params, int hidden, u
     if (cudaDeviceSynchronize() != cudaSuccess) { net_free(t); delete t; return VES_ERR_CUDA; }
     *out = t;
     return VES_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void ves_shiftnet_default_config(ves_shiftnet_config *c)
+{
+    if (!c) return;
+    c->dim = 16;
+    c->n_params = 0;
+    c->hidden = 256;
+    c->layers = 3;
+    c->fourier = 0;
+    c->loss = VES_SHIFTNET_LOSS_CHAMFER;
+    c->delta = 0.01f;
+    c->seed = 0;
+}
+
+int ves_shiftnet_create_config(ves_shiftnet **out, const ves_shiftnet_config *cfg)
+{
+    if (!cfg) return VES_ERR_ARG;
+    return create_from_config(out, *cfg);
+}
+
+int ves_shiftnet_create(ves_shiftnet **out, int dim, int n_params, int hidden, unsigned long long seed)
+{
+    ves_shiftnet_config c;
+    ves_shiftnet_default_config(&c);
+    c.dim = dim;
+    c.n_params = n_params;
+    c.hidden = hidden;
+    c.seed = seed;
+    return create_from_config(out, c);
 }
 
 void ves_shiftnet_destroy(ves_shiftnet *t)
@@ -379,43 +571,45 @@ int ves_shiftnet_train(ves_shiftnet *t, long long count, int thread_cnt, const d
                        const double *iA, const double *rE, const double *iE, int epochs, int batch, float lr,
                        unsigned long long seed, float *loss_per_epoch, void *stream)
 {
-    if (!t || count < 1 || thread_cnt < 1 || (count % thread_cnt) || !rA || !iA || !rE || !iE || epochs < 0 ||
-        batch < 32 || batch > 65536 || !(lr > 0.f))
+    if (!t || count < 1 || count > 0x7fffffffLL || thread_cnt < 1 || (count % thread_cnt) || !rA || !iA || !rE ||
+        !iE || epochs < 0 || batch < 32 || batch > 65536 || !(lr > 0.f))
         return VES_ERR_ARG;
     if (t->P > 0 && !params) return VES_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
-    const int n = t->n;
-    // the whole training set: standardisation statistics first
-    ves::bf16 *Xall = nullptr;
-    float *Tall = nullptr, *Z[4] = {}, *dA = nullptr, *dB = nullptr, *gW[4] = {}, *gb[4] = {}, *loss = nullptr;
-    ves::bf16 *Hs[3] = {}, *Xb = nullptr;
+    const int n = t->n, H = t->H, L = t->L;
+    ves::bf16 *Xall = nullptr, *Xb = nullptr;
+    float *Tall = nullptr, *Tb = nullptr, *dA = nullptr, *dB = nullptr, *loss = nullptr;
+    float *gW[ves::kMaxLayers + 1] = {}, *gb[ves::kMaxLayers + 1] = {};
     int *rows = nullptr, *err = nullptr;
-    const int H = t->H;
+    char *actbuf = nullptr;
+    const int wmax = std::max(H, t->nout_pad);
     bool ok = cudaMalloc(&Xall, (size_t)count * t->kin_pad * 2) == cudaSuccess &&
               cudaMalloc(&Tall, (size_t)count * t->nout_pad * 4) == cudaSuccess &&
               cudaMalloc(&Xb, (size_t)batch * t->kin_pad * 2) == cudaSuccess &&
-              cudaMalloc(&dA, (size_t)batch * 256 * 4) == cudaSuccess &&
-              cudaMalloc(&dB, (size_t)batch * 256 * 4) == cudaSuccess &&
+              cudaMalloc(&Tb, (size_t)batch * t->nout_pad * 4) == cudaSuccess &&
+              cudaMalloc(&dA, (size_t)batch * wmax * 4) == cudaSuccess &&
+              cudaMalloc(&dB, (size_t)batch * wmax * 4) == cudaSuccess &&
               cudaMalloc(&loss, 4 * 2) == cudaSuccess && cudaMalloc(&rows, (size_t)count * 4) == cudaSuccess &&
-              cudaMalloc(&err, 4) == cudaSuccess;
-    for (int l = 0; l < 4 && ok; ++l) {
-        ok &= cudaMalloc(&Z[l], (size_t)batch * t->out[l] * 4) == cudaSuccess;
+              cudaMalloc(&err, 4) == cudaSuccess && cudaMalloc(&actbuf, acts_bytes(t, batch)) == cudaSuccess;
+    for (int l = 0; l <= L && ok; ++l) {
         ok &= cudaMalloc(&gW[l], (size_t)t->out[l] * t->in[l] * 4) == cudaSuccess;
         ok &= cudaMalloc(&gb[l], (size_t)t->out[l] * 4) == cudaSuccess;
-        if (l < 3) ok &= cudaMalloc(&Hs[l], (size_t)batch * H * 2) == cudaSuccess;
     }
-    int rc = VES_OK;
-    if (!ok) rc = VES_ERR_NOMEM;
+    int rc = ok ? VES_OK : VES_ERR_NOMEM;
     if (rc == VES_OK) {
+        char *w = actbuf;
+        const Acts a = carve_acts(t, batch, w);
         cudaMemsetAsync(err, 0, 4, st);
-        ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, t->P, thread_cnt, params, rA, iA, nullptr,
-                                                             nullptr, t->kin, t->kin_pad, Xall, nullptr);
-        ves::colstats_bf16_kernel<<<1, 256, 0, st>>>(count, t->kin_pad, t->kin_pad, Xall, t->fmean, t->fstd);
-        ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, t->P, thread_cnt, params, rA, iA, t->fmean,
-                                                             t->fstd, t->kin, t->kin_pad, Xall, nullptr);
+        // standardisation statistics over the whole training set
+        ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, t->P, t->F, thread_cnt, params, rA, iA,
+                                                             nullptr, nullptr, t->kin, t->kin_pad, Xall, nullptr);
+        ves::colstats_bf16_kernel<<<ves::nb(t->kin_pad), 256, 0, st>>>(count, t->kin_pad, t->kin_pad, Xall, t->fmean,
+                                                                      t->fstd);
+        ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, t->P, t->F, thread_cnt, params, rA, iA,
+                                                             t->fmean, t->fstd, t->kin, t->kin_pad, Xall, nullptr);
         ves::targets_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, thread_cnt, rE, iE, nullptr, nullptr,
                                                             t->nout_pad, Tall, nullptr);
-        ves::colstats_f32_kernel<<<1, 256, 0, st>>>(count, t->nout_pad, t->nout_pad, Tall, t->tmean, t->tstd);
+        ves::target_stats_kernel<<<1, 256, 0, st>>>(count, n, t->nout_pad, t->nout_pad, Tall, t->tmean, t->tstd);
         ves::targets_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, thread_cnt, rE, iE, t->tmean, t->tstd,
                                                             t->nout_pad, Tall, nullptr);
         std::mt19937_64 rng(seed);
@@ -423,45 +617,51 @@ int ves_shiftnet_train(ves_shiftnet *t, long long count, int thread_cnt, const d
         for (long long i = 0; i < count; ++i) perm[i] = (int)i;
         const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
         const long long steps_per_epoch = count / batch;
+        const double total_steps = (double)std::max<long long>(1, steps_per_epoch * epochs);
+        long long k = 0;  // step within this call: cosine decay from lr to lr / 50
         for (int ep = 0; ep < epochs && rc == VES_OK; ++ep) {
             std::shuffle(perm.begin(), perm.end(), rng);
             cudaMemcpyAsync(rows, perm.data(), (size_t)count * 4, cudaMemcpyHostToDevice, st);
             cudaMemsetAsync(loss, 0, 4, st);
             for (long long s = 0; s < steps_per_epoch; ++s) {
                 const int *r = rows + s * batch;
-                // gather the batch: features, targets
-                ves::features_kernel<<<ves::nb(batch), 256, 0, st>>>(batch, n, t->P, thread_cnt, params, rA, iA,
-                                                                     t->fmean, t->fstd, t->kin, t->kin_pad, Xb, r);
-                float *Tb = dB;  // targets of the batch (reuse buffer; overwritten after the loss)
+                ves::features_kernel<<<ves::nb(batch), 256, 0, st>>>(batch, n, t->P, t->F, thread_cnt, params, rA,
+                                                                     iA, t->fmean, t->fstd, t->kin, t->kin_pad, Xb, r);
                 ves::targets_kernel<<<ves::nb(batch), 256, 0, st>>>(batch, n, thread_cnt, rE, iE, t->tmean, t->tstd,
                                                                     t->nout_pad, Tb, r);
-                forward(t, batch, Xb, Z, Hs, err, st);
-                // dY into dA
-                ves::mse_kernel<<<ves::nb((long long)batch * t->nout_pad), 256, 0, st>>>(
-                    batch, t->nout_pad, t->nout, Z[3], Tb, dA, loss);
-                // backward through layers 3..0; dA holds dZ of the current layer
-                float *dZ = dA, *dH = dB;
-                for (int l = 3; l >= 0; --l) {
-                    const ves::bf16 *Hin = l == 0 ? Xb : Hs[l - 1];
+                forward(t, batch, Xb, a, err, st);
+                ves::chamfer_kernel<<<ves::nb(batch, 128), 128, 0, st>>>(batch, n, t->nout_pad, a.Y, Tb, dA, loss,
+                                                                         t->cfg.loss, t->cfg.delta);
+                // output layer (FP32): dW = dY^T Hf, dH = dY W, then through GELU
+                ves::dw_kernel<float><<<dim3(ves::nb(H, 128), t->nout_pad), 128, 0, st>>>(
+                    batch, t->nout_pad, H, dA, a.Hf, H, gW[L], gb[L]);
+                ves::dh_kernel<<<dim3(ves::nb(H, 128), batch), 128, 0, st>>>(batch, t->nout_pad, H, dA, t->W[L], dB);
+                ves::gelu_bwd_kernel<<<ves::nb((long long)batch * H), 256, 0, st>>>((long long)batch * H, dB,
+                                                                                    a.Z[L - 1], dB);
+                // hidden layers L-1 .. 0; dZ holds the gradient of the current layer's pre-activation
+                float *dZ = dB, *dH = dA;
+                for (int l = L - 1; l >= 0; --l) {
+                    const ves::bf16 *Hin = l == 0 ? Xb : a.Hs[l - 1];
                     const int ldh = l == 0 ? t->kin_pad : H;
-                    ves::dw_kernel<<<dim3(ves::nb(t->in[l], 128), t->out[l]), 128, 0, st>>>(
-                        batch, t->out[l], t->in[l], dZ, Hin, ldh, gW[l], gb[l]);
+                    ves::dw_kernel<ves::bf16><<<dim3(ves::nb(t->in[l], 128), H), 128, 0, st>>>(
+                        batch, H, t->in[l], dZ, Hin, ldh, gW[l], gb[l]);
                     if (l > 0) {
-                        ves::dh_kernel<<<dim3(ves::nb(t->in[l], 128), batch), 128, 0, st>>>(batch, t->out[l],
-                                                                                            t->in[l], dZ, t->W[l], dH);
+                        ves::dh_kernel<<<dim3(ves::nb(H, 128), batch), 128, 0, st>>>(batch, H, H, dZ, t->W[l], dH);
                         ves::gelu_bwd_kernel<<<ves::nb((long long)batch * H), 256, 0, st>>>((long long)batch * H, dH,
-                                                                                            Z[l - 1], dH);
+                                                                                            a.Z[l - 1], dH);
                         float *tmp = dZ; dZ = dH; dH = tmp;
                     }
                 }
                 ++t->step;
+                const float lr_k = (float)(lr * (0.02 + 0.49 * (1.0 + std::cos(3.141592653589793 * (double)k++ /
+                                                                                 total_steps))));
                 const float c1 = 1.f - std::pow(b1, (float)t->step), c2 = 1.f - std::pow(b2, (float)t->step);
-                for (int l = 0; l < 4; ++l) {
+                for (int l = 0; l <= L; ++l) {
                     const long long nw = (long long)t->out[l] * t->in[l];
-                    ves::adam_kernel<<<ves::nb(nw), 256, 0, st>>>(nw, t->W[l], gW[l], t->mW[l], t->vW[l], lr, b1, b2,
-                                                                 eps, c1, c2, t->Wb[l]);
+                    ves::adam_kernel<<<ves::nb(nw), 256, 0, st>>>(nw, t->W[l], gW[l], t->mW[l], t->vW[l], lr_k, b1, b2,
+                                                                 eps, c1, c2, l < L ? t->Wb[l] : nullptr);
                     ves::adam_kernel<<<ves::nb(t->out[l]), 256, 0, st>>>(t->out[l], t->b[l], gb[l], t->mb[l],
-                                                                        t->vb[l], lr, b1, b2, eps, c1, c2, nullptr);
+                                                                        t->vb[l], lr_k, b1, b2, eps, c1, c2, nullptr);
                 }
             }
             float lh = 0.f;
@@ -474,9 +674,9 @@ int ves_shiftnet_train(ves_shiftnet *t, long long count, int thread_cnt, const d
         if (he) rc = VES_ERR_CUDA;
         if (cudaDeviceSynchronize() != cudaSuccess) rc = VES_ERR_CUDA;
     }
-    cudaFree(Xall); cudaFree(Tall); cudaFree(Xb); cudaFree(dA); cudaFree(dB); cudaFree(loss); cudaFree(rows);
-    cudaFree(err);
-    for (int l = 0; l < 4; ++l) { cudaFree(Z[l]); cudaFree(gW[l]); cudaFree(gb[l]); if (l < 3) cudaFree(Hs[l]); }
+    cudaFree(Xall); cudaFree(Tall); cudaFree(Xb); cudaFree(Tb); cudaFree(dA); cudaFree(dB); cudaFree(loss);
+    cudaFree(rows); cudaFree(err); cudaFree(actbuf);
+    for (int l = 0; l <= L; ++l) { cudaFree(gW[l]); cudaFree(gb[l]); }
     return rc;
 }
 
@@ -484,49 +684,50 @@ size_t ves_shiftnet_predict_workspace_size(const ves_shiftnet *t, long long coun
 {
     if (!t || count < 0) return 0;
     const size_t rows = (size_t)count;
-    return rows * t->kin_pad * 2 + 3 * rows * t->H * 2 + rows * (3 * (size_t)t->H + t->nout_pad) * 4 + 8 * 256;
+    return ((rows * t->kin_pad * 2 + 255) & ~(size_t)255) + acts_bytes(t, rows) + 256;
 }
 
 int ves_shiftnet_predict(const ves_shiftnet *t, long long count, int thread_cnt, const double *params,
                          const double *rA, const double *iA, double *rS, double *iS, void *workspace,
                          size_t workspace_bytes, void *stream)
 {
-    if (!t || count < 0 || thread_cnt < 1 || (count % thread_cnt) || !rA || !iA || !rS || !iS) return VES_ERR_ARG;
+    if (!t || count < 0 || count > 0x7fffffffLL || thread_cnt < 1 || (count % thread_cnt) || !rA || !iA || !rS ||
+        !iS)
+        return VES_ERR_ARG;
     if (t->P > 0 && !params) return VES_ERR_ARG;
     if (count == 0) return VES_OK;
     if (!workspace || workspace_bytes < ves_shiftnet_predict_workspace_size(t, count)) return VES_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     char *w = static_cast<char *>(workspace);
-    auto take = [&](size_t bytes) { char *p = w; w += (bytes + 255) & ~(size_t)255; return p; };
-    ves::bf16 *X = reinterpret_cast<ves::bf16 *>(take((size_t)count * t->kin_pad * 2));
-    ves::bf16 *Hs[3];
-    for (int l = 0; l < 3; ++l) Hs[l] = reinterpret_cast<ves::bf16 *>(take((size_t)count * t->H * 2));
-    float *Z[4];
-    for (int l = 0; l < 4; ++l) Z[l] = reinterpret_cast<float *>(take((size_t)count * t->out[l] * 4));
-    int *err = nullptr;  // the GEMM's completion flag is checked in training; inference trusts it
-    ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, t->n, t->P, thread_cnt, params, rA, iA, t->fmean,
-                                                         t->fstd, t->kin, t->kin_pad, X, nullptr);
-    if (forward(t, (int)count, X, Z, Hs, err, st) != cudaSuccess) return VES_ERR_CUDA;
-    ves::shifts_out_kernel<<<ves::nb(count), 256, 0, st>>>(count, t->n, thread_cnt, t->nout_pad, Z[3], t->tmean,
+    ves::bf16 *X = reinterpret_cast<ves::bf16 *>(w);
+    w += ((size_t)count * t->kin_pad * 2 + 255) & ~(size_t)255;
+    const Acts a = carve_acts(t, (size_t)count, w);
+    int *err = nullptr;  // a GEMM wait that gives up leaves its tile unwritten; training checks the flag
+    ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, t->n, t->P, t->F, thread_cnt, params, rA, iA,
+                                                         t->fmean, t->fstd, t->kin, t->kin_pad, X, nullptr);
+    if (forward(t, (int)count, X, a, err, st) != cudaSuccess) return VES_ERR_CUDA;
+    ves::shifts_out_kernel<<<ves::nb(count), 256, 0, st>>>(count, t->n, thread_cnt, t->nout_pad, a.Y, t->tmean,
                                                            t->tstd, rS, iS);
     return cudaGetLastError() == cudaSuccess ? VES_OK : VES_ERR_CUDA;
 }
 
-// Flat binary checkpoint: header (magic, version, n, P, H, step) then, per
-// layer, W and b (FP32), then the four normalisation vectors.
+// Flat binary checkpoint: header {magic, version 2, n, P, H, L, F, loss, step},
+// delta (float), seed (u64), then per layer W and b (FP32), then the four
+// normalisation vectors.
 int ves_shiftnet_save(const ves_shiftnet *t, const char *path)
 {
     if (!t || !path) return VES_ERR_ARG;
     FILE *f = fopen(path, "wb");
     if (!f) return VES_ERR_ARG;
-    const int hdr[6] = {0x56455353, 1, t->n, t->P, t->H, (int)t->step};
-    bool ok = fwrite(hdr, sizeof hdr, 1, f) == 1;
+    const int hdr[9] = {0x56455353, 2, t->n, t->P, t->H, t->L, t->F, t->cfg.loss, (int)t->step};
+    bool ok = fwrite(hdr, sizeof hdr, 1, f) == 1 && fwrite(&t->cfg.delta, 4, 1, f) == 1 &&
+              fwrite(&t->cfg.seed, 8, 1, f) == 1;
     auto put = [&](const float *d, size_t cnt) {
         std::vector<float> h(cnt);
         ok = ok && cudaMemcpy(h.data(), d, cnt * 4, cudaMemcpyDeviceToHost) == cudaSuccess &&
              fwrite(h.data(), 4, cnt, f) == cnt;
     };
-    for (int l = 0; l < 4; ++l) {
+    for (int l = 0; l <= t->L; ++l) {
         put(t->W[l], (size_t)t->out[l] * t->in[l]);
         put(t->b[l], t->out[l]);
     }
@@ -540,23 +741,30 @@ int ves_shiftnet_load(ves_shiftnet **out, const char *path)
     if (!out || !path) return VES_ERR_ARG;
     FILE *f = fopen(path, "rb");
     if (!f) return VES_ERR_ARG;
-    int hdr[6];
-    if (fread(hdr, sizeof hdr, 1, f) != 1 || hdr[0] != 0x56455353 || hdr[1] != 1) { fclose(f); return VES_ERR_ARG; }
+    int hdr[9];
+    ves_shiftnet_config c;
+    ves_shiftnet_default_config(&c);
+    if (fread(hdr, sizeof hdr, 1, f) != 1 || hdr[0] != 0x56455353 || hdr[1] != 2 || fread(&c.delta, 4, 1, f) != 1 ||
+        fread(&c.seed, 8, 1, f) != 1) {
+        fclose(f);
+        return VES_ERR_ARG;
+    }
+    c.dim = hdr[2]; c.n_params = hdr[3]; c.hidden = hdr[4]; c.layers = hdr[5]; c.fourier = hdr[6]; c.loss = hdr[7];
     ves_shiftnet *t = nullptr;
-    int rc = ves_shiftnet_create(&t, hdr[2], hdr[3], hdr[4], 0);
+    int rc = create_from_config(&t, c);
     if (rc != VES_OK) { fclose(f); return rc; }
-    t->step = hdr[5];
+    t->step = hdr[8];
     bool ok = true;
     auto get = [&](float *d, size_t cnt) {
         std::vector<float> h(cnt);
         ok = ok && fread(h.data(), 4, cnt, f) == cnt &&
              cudaMemcpy(d, h.data(), cnt * 4, cudaMemcpyHostToDevice) == cudaSuccess;
     };
-    for (int l = 0; l < 4; ++l) {
+    for (int l = 0; l <= t->L; ++l) {
         get(t->W[l], (size_t)t->out[l] * t->in[l]);
         get(t->b[l], t->out[l]);
         const long long nw = (long long)t->out[l] * t->in[l];
-        ves::to_bf16_kernel<<<ves::nb(nw), 256>>>(nw, t->W[l], t->Wb[l]);
+        if (l < t->L) ves::to_bf16_kernel<<<ves::nb(nw), 256>>>(nw, t->W[l], t->Wb[l]);
     }
     get(t->fmean, t->kin_pad); get(t->fstd, t->kin_pad); get(t->tmean, t->nout_pad); get(t->tstd, t->nout_pad);
     fclose(f);

@@ -47,16 +47,17 @@ def solve_plain(n, N, rA, iA, thread_cnt=512, vectors=False):
     return rE, iE, sw
 
 
-def train(n, count=200_000, epochs=30, batch=1024, lr=1e-3, hidden=256, family_seed=4, param_seed=5, seed=0,
-          thread_cnt=512):
+def train(n, count=200_000, epochs=60, batch=1024, lr=1e-3, hidden=256, family_seed=4, param_seed=5, seed=0,
+          thread_cnt=512, **config):
     """Train a ShiftNet for order n on `count` plain-solver solutions (rounded
-    down to a multiple of thread_cnt)."""
+    down to a multiple of thread_cnt); `config` passes ves_shiftnet_config
+    fields (layers, fourier, loss, delta)."""
     import torch
     count = max(thread_cnt, count // thread_cnt * thread_cnt)
     p, rA, iA = family(count, n, family_seed, param_seed, thread_cnt)
     rE, iE, _ = solve_plain(n, count, rA, iA, thread_cnt)
     torch.cuda.synchronize()
-    net = ves.ShiftNet(dim=n, n_params=3, hidden=hidden, seed=seed)
+    net = ves.ShiftNet(dim=n, n_params=3, hidden=hidden, seed=seed, **config)
     losses = net.train(count, thread_cnt, p, rA, iA, rE, iE, epochs=epochs, batch=batch, lr=lr, seed=seed)
     return net, losses
 
@@ -74,3 +75,30 @@ def prediction_error(n, N, rS, iS, rE, iE, thread_cnt=512):
     S = ves.complex_vec_from_soa(rS.cpu().numpy(), iS.cpu().numpy(), n, thread_cnt)
     E = ves.complex_vec_from_soa(rE.cpu().numpy(), iE.cpu().numpy(), n, thread_cnt)
     return np.abs(S[:, :, None] - E[:, None, :]).min(axis=2)
+
+
+def relative_error(n, rA, iA, rS, iS, rE, iE, thread_cnt=512):
+    """Per true eigenvalue, the distance to the nearest prediction in units of
+    ||A||_F / sqrt(n) (the units of ves_options.shift_gate); a device tensor
+    (N, n)."""
+    import torch
+
+    def vec(re, im):
+        return torch.complex(re.view(-1, n, thread_cnt), im.view(-1, n, thread_cnt)).permute(0, 2, 1).reshape(-1, n)
+    S, E = vec(rS, iS), vec(rE, iE)
+    fro = torch.linalg.vector_norm(torch.complex(rA.view(-1, n * n, thread_cnt), iA.view(-1, n * n, thread_cnt)),
+                                   dim=1).reshape(-1)
+    d = (E[:, :, None] - S[:, None, :]).abs().amin(dim=2)
+    return d / (fro[:, None] / np.sqrt(n))
+
+
+def calibrate(net, n, count=32768, family_seed=4, param_seed=7, thread_cnt=512, factor=1.0):
+    """The gate for ves_options.shift_gate: `factor` x the median prediction
+    error (relative_error) on a held-out draw of the family."""
+    import torch
+    p, rA, iA = family(count, n, family_seed, param_seed, thread_cnt)
+    rE, iE, _ = solve_plain(n, count, rA, iA, thread_cnt)
+    rS, iS = predict(net, n, count, p, rA, iA, thread_cnt)
+    torch.cuda.synchronize()
+    err = relative_error(n, rA, iA, rS, iS, rE, iE, thread_cnt)
+    return factor * float(err.median())

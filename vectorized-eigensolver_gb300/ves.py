@@ -34,10 +34,18 @@ class VesError(RuntimeError):
     pass
 
 
+class ShiftNetConfig(ctypes.Structure):
+    _fields_ = [("dim", _int), ("n_params", _int), ("hidden", _int), ("layers", _int), ("fourier", _int),
+                ("loss", _int), ("delta", ctypes.c_float), ("seed", ctypes.c_ulonglong)]
+
+
+VES_SHIFTNET_LOSS_CHAMFER, VES_SHIFTNET_LOSS_ROBUST = 0, 1
+
+
 class Options(ctypes.Structure):
     _fields_ = [("precision", _int), ("max_its", _int), ("vnorm", _int), ("refine_steps", _int),
                 ("refine_tol", _dbl), ("want_vectors", _int), ("blocks_per_sm", _int), ("varsize_order", _int),
-                ("shift_sweeps", _int), ("reserved", _int * 2)]
+                ("shift_sweeps", _int), ("shift_gate", ctypes.c_float), ("reserved", _int)]
 
 
 # exported symbol -> (restype, argtypes); every name declared in include/ves.h
@@ -76,6 +84,8 @@ SIGNATURES = {
     "ves_eigensolve_shifts": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
                                      ctypes.POINTER(Options), _VP, _size, _VP]),
     "ves_shiftnet_create": (_int, [ctypes.POINTER(_VP), _int, _int, _int, ctypes.c_ulonglong]),
+    "ves_shiftnet_default_config": (None, [ctypes.POINTER(ShiftNetConfig)]),
+    "ves_shiftnet_create_config": (_int, [ctypes.POINTER(_VP), ctypes.POINTER(ShiftNetConfig)]),
     "ves_shiftnet_destroy": (None, [_VP]),
     "ves_shiftnet_train": (_int, [_VP, ctypes.c_longlong, _int, _VP, _VP, _VP, _VP, _VP, _int, _int,
                                   ctypes.c_float, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_float), _VP]),
@@ -381,13 +391,19 @@ def eigensolve_shifts(dim, block_cnt, thread_cnt, rA, iA, rE, iE, rV, iV, rS, iS
 class ShiftNet:
     """The learned-shift network (ves_shiftnet_*): features -> predicted eigenvalues."""
 
-    def __init__(self, dim=None, n_params=0, hidden=256, seed=0, path=None):
+    def __init__(self, dim=None, n_params=0, hidden=256, seed=0, path=None, **config):
+        """config: layers, fourier, loss, delta (ves_shiftnet_config fields)."""
         self.handle = _VP()
         if path is not None:
             _check(lib().ves_shiftnet_load(ctypes.byref(self.handle), path.encode()), "ves_shiftnet_load")
         else:
-            _check(lib().ves_shiftnet_create(ctypes.byref(self.handle), dim, n_params, hidden, seed),
-                   "ves_shiftnet_create")
+            c = ShiftNetConfig()
+            lib().ves_shiftnet_default_config(ctypes.byref(c))
+            c.dim, c.n_params, c.hidden, c.seed = dim, n_params, hidden, seed
+            for k, v in config.items():
+                setattr(c, k, v)
+            _check(lib().ves_shiftnet_create_config(ctypes.byref(self.handle), ctypes.byref(c)),
+                   "ves_shiftnet_create_config")
 
     def train(self, count, thread_cnt, params, rA, iA, rE, iE, epochs=20, batch=1024, lr=1e-3, seed=0, stream=None):
         losses = (ctypes.c_float * max(epochs, 1))()

@@ -60,20 +60,27 @@ def gaussian_soa(N, n, seed, thread_cnt):
     return planes[0], planes[1]
 
 
-def _unitary(gen, k, n, device):
-    """k random dense unitaries H(u) H(w) diag(phases), H(x) = I - 2 x x^H / |x|^2:
-    cheap to form (no factorisation), dense, exactly unitary."""
+def _haar(gen, k, n, device):
+    """k Haar-distributed n x n unitaries as a product of n - 1 Householder
+    reflections with complex Gaussian vectors of decreasing length and a
+    diagonal of uniform phases (Stewart 1980, "The efficient generation of
+    random orthogonal matrices"); batched matrix products only."""
     import torch
-
-    def refl():
-        x = torch.complex(torch.randn(k, n, generator=gen, dtype=torch.float64, device=device),
-                          torch.randn(k, n, generator=gen, dtype=torch.float64, device=device))
-        x = x / torch.linalg.vector_norm(x, dim=1, keepdim=True)
-        return torch.eye(n, dtype=torch.complex128, device=device)[None] - 2 * x[:, :, None] * x.conj()[:, None, :]
-
-    ph = torch.polar(torch.ones(k, n, dtype=torch.float64, device=device),
-                     2 * np.pi * torch.rand(k, n, generator=gen, dtype=torch.float64, device=device))
-    return (refl() @ refl()) * ph[:, None, :]
+    U = torch.eye(n, dtype=torch.complex128, device=device).repeat(k, 1, 1)
+    for j in range(n - 1):
+        m = n - j
+        x = torch.complex(torch.randn(k, m, generator=gen, dtype=torch.float64, device=device),
+                          torch.randn(k, m, generator=gen, dtype=torch.float64, device=device))
+        a = x[:, 0]
+        ph = torch.where(a.abs() > 0, a / a.abs().clamp_min(1e-300), torch.ones_like(a))
+        v = x.clone()
+        v[:, 0] = a + ph * torch.linalg.vector_norm(x, dim=1)
+        v = v / torch.linalg.vector_norm(v, dim=1, keepdim=True)
+        Uc = U[:, :, j:]
+        U[:, :, j:] = Uc - 2 * (Uc @ v[:, :, None]) * v.conj()[:, None, :]
+    d = torch.polar(torch.ones(k, n, dtype=torch.float64, device=device),
+                    2 * np.pi * torch.rand(k, n, generator=gen, dtype=torch.float64, device=device))
+    return U * d[:, None, :]
 
 
 def _similar(U, s, W, lam):
@@ -84,15 +91,30 @@ def _similar(U, s, W, lam):
     return (V * lam[:, None, :]) @ Vinv
 
 
+def _inverse_near_unitary(X, U, iters=10):
+    """X^-1 for X = U + E with U unitary and ||E||_2 < 1: Newton-Schulz
+    iteration Y <- Y (2I - X Y) from Y = U^H (quadratic convergence from
+    ||I - X U^H|| = ||E||)."""
+    import torch
+    Y = U.conj().transpose(1, 2)
+    two = 2 * torch.eye(X.shape[-1], dtype=X.dtype, device=X.device)
+    for _ in range(iters):
+        Y = Y @ (two - X @ Y)
+    return Y
+
+
 def mixed_families(N, seed=2, nmin=4, nmax=64, device="cpu", as_list=True):
     """The mixed-size workload: N complex128 matrices, order uniform in
     [nmin, nmax], matrix m of family m % 3:
       0  i.i.d. complex Gaussian;
       1  non-normal A = V diag(l) V^-1, V = U diag(logspace(0, -4, n)) W with U, W
-         random dense unitaries (cond(V) = 1e4), l uniform in the unit disk;
-      2  clustered A = X diag(l) X^-1, X = U diag(logspace(0, -1, n)) W (cond 10),
-         l = one of 4 complex-Gaussian centres plus an offset uniform in a disk of
-         radius 1e-6.
+         Haar unitaries (cond(V) = 1e4, V^-1 = W^H diag(1/s) U^H exactly),
+         l uniform in the unit disk (r = sqrt(u));
+      2  clustered A = X diag(l) X^-1, X = U + 0.3 G / sqrt(n) (U Haar, G complex
+         Gaussian with E|g|^2 = 1; ||X - U||_2 is about 0.6, so X is well conditioned and
+         X^-1 comes from a Newton-Schulz iteration started at U^H),
+         l = one of 4 complex-Gaussian centres plus an offset uniform in a disk
+         of radius 1e-6.
     Generated with torch (seeded), batched by order, matrix products only.
     Returns a list of (n, n) numpy arrays (as_list) or (sizes, dict n -> (indices,
     tensor))."""
@@ -117,7 +139,7 @@ def mixed_families(N, seed=2, nmin=4, nmax=64, device="cpu", as_list=True):
             s = torch.logspace(0, -4, n, dtype=torch.float64, device=device).to(torch.complex128)
             r = torch.sqrt(torch.rand(c, n, generator=gen, dtype=torch.float64, device=device))
             th = 2 * np.pi * torch.rand(c, n, generator=gen, dtype=torch.float64, device=device)
-            out[g] = _similar(_unitary(gen, c, n, device), s, _unitary(gen, c, n, device), torch.polar(r, th))
+            out[g] = _similar(_haar(gen, c, n, device), s, _haar(gen, c, n, device), torch.polar(r, th))
         g = f == 2
         if g.any():
             c = int(g.sum())
@@ -126,8 +148,11 @@ def mixed_families(N, seed=2, nmin=4, nmax=64, device="cpu", as_list=True):
             r = 1e-6 * torch.sqrt(torch.rand(c, n, generator=gen, dtype=torch.float64, device=device))
             th = 2 * np.pi * torch.rand(c, n, generator=gen, dtype=torch.float64, device=device)
             lam = centres[:, torch.arange(n, device=device) % 4] + torch.polar(r, th)
-            s = torch.logspace(0, -1, n, dtype=torch.float64, device=device).to(torch.complex128)
-            out[g] = _similar(_unitary(gen, c, n, device), s, _unitary(gen, c, n, device), lam)
+            U = _haar(gen, c, n, device)
+            G = torch.complex(torch.randn(c, n, n, generator=gen, dtype=torch.float64, device=device),
+                              torch.randn(c, n, n, generator=gen, dtype=torch.float64, device=device))
+            X = U + (0.3 / np.sqrt(2 * n)) * G
+            out[g] = (X * lam[:, None, :]) @ _inverse_near_unitary(X, U)
         by_n[int(n)] = (idx, out)
     if not as_list:
         return sizes, by_n
