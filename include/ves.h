@@ -131,7 +131,8 @@ typedef struct ves_options {
     float shift_gate;  /* ves_eigensolve_shifts: an eigenvalue uses the predictions only while its subdiagonal
                         * |H(I,I-1)| exceeds shift_gate * ||A||_F / sqrt(n) (below that the Wilkinson shift
                         * is the better estimate); set it to the predictor's typical error; default 0 */
-    int reserved;
+    int shift_polish;  /* ves_eigensolve_shifts: Newton steps on det(H - sI) (FP32, Hyman's recurrence on the
+                        * Hessenberg matrix) that refine each prediction before the QR; 0 (default) = none */
 } ves_options;
 
 void ves_default_options(ves_options *opt);

@@ -61,3 +61,27 @@ def test_tuned_shape_same_results(tmp_path, precision):
     for other in outs[1:]:
         for a, b in zip(outs[0], other):
             assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_tune_varsize_same_results(tmp_path):
+    """The mixed-size tuner picks among (blocks_per_sm, order); every choice
+    gives the same eigenvalues and eigenvectors."""
+    import torch
+    import workloads
+    c = autotune.TuneCache(str(tmp_path / "t.json"))
+    sizes, by_n = workloads.mixed_families(1500, seed=4, nmax=24, device="cuda", as_list=False)
+    e = autotune.tune_varsize(sizes, by_n, max_dim=24, candidates=(1, 3), orders=(0, 1), reps=1, cache=c)
+    assert (e["blocks_per_sm"], e["varsize_order"]) in {(1, 0), (3, 0), (1, 1), (3, 1)}
+    dims, re, im = workloads.pack_varsize(sizes, by_n, device="cuda")
+    outs = []
+    for b, order in ((1, 0), (3, 1), (0, 0)):
+        o = ves.default_options(blocks_per_sm=b, varsize_order=order)
+        er = torch.empty(int(sizes.sum()), dtype=torch.float64, device="cuda")
+        ei, vr, vi = torch.empty_like(er), torch.empty_like(re), torch.empty_like(im)
+        ves.eigensolve_varsize(len(sizes), 24, dims, re, im, er, ei, vr, vi, options=o)
+        torch.cuda.synchronize()
+        outs.append([t.cpu().numpy() for t in (er, ei, vr, vi)])
+    for other in outs[1:]:
+        for a, b in zip(outs[0], other):
+            assert np.array_equal(a, b)

@@ -124,6 +124,33 @@ def test_structured_and_degenerate_inputs():
                                atol=1e-13 * np.abs(real_upper).max())
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_hermitian_and_unitary_inputs(precision):
+    """Normal matrices: Hermitian (real spectrum) and unitary (spectrum on the
+    unit circle); eigenvalues within the bar, every residual within the bar,
+    eigenvectors of separated eigenvalues orthogonal."""
+    rng = np.random.default_rng(5)
+    n, N = 12, 64
+    G = cgauss(rng, (N, n, n))
+    herm = (G + np.conj(np.swapaxes(G, 1, 2))) / 2
+    Q, _ = np.linalg.qr(cgauss(rng, (N, n, n)))
+    A = np.concatenate([herm[:32], Q[:32]])
+    out = run_fused(A, 32, precision=precision)
+    w = np.linalg.eigvals(A)
+    _, err, _ = match_eigs(out["E"], w)
+    nA = np.linalg.norm(A, axis=(1, 2))
+    assert (err / nA).max() <= EIG_TOL
+    assert np.abs(out["E"][:32].imag).max() <= 1e-13 * nA[:32].max()
+    np.testing.assert_allclose(np.abs(out["E"][32:]), 1.0, atol=1e-13)
+    assert residuals(A, out["E"], out["V"]).max() <= RES_TOL
+    V = out["V"] / np.linalg.norm(out["V"], axis=1, keepdims=True)
+    gram = np.abs(np.conj(np.swapaxes(V, 1, 2)) @ V - np.eye(n))
+    well = separation(w) / nA[:, None] > 1e-3
+    for m in range(N):
+        if well[m].all():
+            assert gram[m].max() <= 1e-9
+
+
 def test_nonfinite_input_flagged():
     rng = np.random.default_rng(4)
     A = cgauss(rng, (64, 5, 5))

@@ -1,5 +1,7 @@
 """The learned-shift network's BF16 GEMM on the tcgen05 tensor cores against a
-plain fp32 product of the same BF16 values."""
+plain fp32 product of the same BF16 values.  Shapes with K <= 256, K % 16 == 0
+and N % 16 == 0 run the persistent kernel (weights resident in shared memory,
+whole-K tiles); the others the K-chunked kernel."""
 import pytest
 
 import ves
@@ -8,7 +10,8 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("M,N,K", [(128, 256, 64), (300, 256, 64), (1024, 256, 256), (77, 48, 256), (512, 64, 96),
-                                   (5, 16, 32)])
+                                   (5, 16, 32), (20000, 256, 256), (3000, 128, 192),
+                                   (256, 256, 264), (100, 24, 40), (130, 80, 8)])
 @pytest.mark.parametrize("act", [0, 1])
 def test_gemm_bf16_matches_fp32_reference(M, N, K, act):
     import torch

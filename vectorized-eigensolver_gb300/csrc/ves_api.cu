@@ -492,6 +492,7 @@ void ves_default_options(ves_options *opt)
     opt->varsize_order = 0;
     opt->shift_sweeps = 1;
     opt->shift_gate = 0.f;
+    opt->shift_polish = 0;
 }
 
 size_t ves_eigensolve_workspace_size(int dim, int block_cnt, int thread_cnt, const ves_options *opt)
@@ -691,11 +692,11 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *
     if (opt) o = *opt;
     if (o.max_its < 0 || o.max_its > 10000 || o.vnorm < 0 || o.vnorm > 2 || o.shift_sweeps < 0 ||
         o.shift_sweeps > 9 || o.blocks_per_sm < 0 || o.blocks_per_sm > 16 || !(o.shift_gate >= 0.f) ||
-        o.shift_gate > 1e6f) {
+        o.shift_gate > 1e6f || o.shift_polish < 0 || o.shift_polish > 16) {
         set_error("option out of range");
         return VES_ERR_ARG;
     }
-    const size_t need = align256(ves::fused_workspace_bytes(dim, g.N, o.blocks_per_sm, nullptr, nullptr));
+    const size_t need = align256(ves::fused_workspace_bytes(dim, g.N, o.blocks_per_sm, nullptr, nullptr, true));
     void *ws = workspace;
     std::unique_lock<std::mutex> lk;
     if (!ws) {
@@ -716,6 +717,7 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *
     a.rS = rS; a.iS = iS;
     a.shift_sweeps = o.shift_sweeps;
     a.shift_gate = o.shift_gate;
+    a.shift_polish = o.shift_polish;
     a.fallbacks = fallbacks;
     a.blocks_per_sm = o.blocks_per_sm;
     return native(cuda_ok(ves::launch_fused_fp64(a, (cudaStream_t)stream), "learned-shift solve launch"));

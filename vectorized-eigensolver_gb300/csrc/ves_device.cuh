@@ -133,6 +133,16 @@ template <> struct lim<float> {
 
 // The reference's structure-of-arrays layout: two planes, element (i,j) of a
 // matrix at ((i-1) + (j-1)*n) * s from the matrix's base (s = thread_cnt).
+// Bit test for Inf/NaN without touching the FP64 pipe.
+__device__ __forceinline__ bool nonfinite(double v)
+{
+    return (__double2hiint(v) & 0x7ff00000) == 0x7ff00000;
+}
+__device__ __forceinline__ bool nonfinite(float v)
+{
+    return (__float_as_uint(v) & 0x7f800000u) == 0x7f800000u;
+}
+
 template <class R> struct MatSoA {
     R *re, *im;
     long long s;
@@ -425,8 +435,7 @@ struct NoShiftPredictions {
 // starts: once it is that small the Wilkinson shift is already more accurate
 // than the predictions, and they are left alone.
 struct ShiftPredictions {
-    const double *re, *im;  // this matrix's predictions, stride s
-    long long s;
+    VecIlv<double> S;  // this matrix's n predictions in the workspace (NaN: none)
     int n, sweeps;
     double gate;
     unsigned long long used;
@@ -441,7 +450,9 @@ struct ShiftPredictions {
                 int bi = -1;
                 for (int k = 0; k < n; ++k) {
                     if ((used >> k) & 1ULL) continue;
-                    const R dr = (R)re[k * s] - t.r, di = (R)im[k * s] - t.i;
+                    const cx<double> p = S.ld(k + 1);
+                    if (p.r != p.r) continue;  // dropped prediction
+                    const R dr = (R)p.r - t.r, di = (R)p.i - t.i;
                     const R d = dr * dr + di * di;
                     if (bi < 0 || d < best) { best = d; bi = k; }
                 }
@@ -450,11 +461,89 @@ struct ShiftPredictions {
             }
         }
         if (its >= sweeps || its == 10 || its == 20) return;
-        if (current >= 0) t = mk((R)re[current * s], (R)im[current * s]);
+        if (current >= 0) {
+            const cx<double> p = S.ld(current + 1);
+            t = mk((R)p.r, (R)p.i);
+        }
     }
     // a predicted eigenvalue that still needed more than sweeps + 2 sweeps
     __device__ __forceinline__ void deflated(int its) { if (current >= 0 && its > sweeps + 2) ++fallbacks; }
 };
+
+// Newton's method on det(H - s I) for the upper Hessenberg H, in FP32 on Hf
+// (an FP32 copy of H), by Hyman's recurrence: with x_n = 1,
+//     x_{i-1} = -[(h_ii - s) x_i + sum_{j>i} h_ij x_j] / h_{i,i-1},   i = n..2,
+//     r(s)    = (h_11 - s) x_1 + sum_{j>1} h_1j x_j,
+// det(H - s I) = c r(s) with c independent of s, so a Newton step is r / r',
+// r' from the differentiated recurrence (x, x' are rescaled together when
+// they grow: the ratio does not depend on their common scale).  Each
+// prediction in S gets up to `steps` steps, stopping once a step is below
+// `tol`.  A prediction is kept only if its last step was below `keep` (the
+// iteration has reached its quadratic phase): one that has not converged, or
+// whose iteration broke down (a zero subdiagonal, non-finite values), or that
+// lands within `dup` of an earlier one is dropped (NaN), and its eigenvalue is
+// found with the Wilkinson shift -- a far prediction costs sweeps, a dropped
+// one costs nothing.  The FP32 pipe does this work at a small fraction of one
+// FP64 QR sweep.
+template <int MAXN>
+__device__ void polish_shifts_lane(const int n, const MatIlv<float> &Hf, const VecIlv<double> &S, const int steps,
+                                   const float tol, const float keep, const float dup)
+{
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    cx<float> x[MAXN], dx[MAXN];
+    for (int k = 1; k <= n; ++k) {
+        const cx<double> s0 = S.ld(k);
+        cx<float> s = mk((float)s0.r, (float)s0.i);
+        bool ok = !nonfinite(s.r) && !nonfinite(s.i) && n >= 2;
+        float last = 3.0e38f;
+        for (int it = 0; it < steps && ok; ++it) {
+            x[n - 1] = mk(1.f, 0.f);
+            dx[n - 1] = mk(0.f, 0.f);
+            for (int i = n; i >= 2; --i) {
+                const cx<float> d = csub(Hf.ld(i, i), s);
+                cx<float> acc = cmul(d, x[i - 1]);
+                cx<float> dacc = csub(cmul(d, dx[i - 1]), x[i - 1]);
+                for (int j = i + 1; j <= n; ++j) {
+                    const cx<float> h = Hf.ld(i, j);
+                    acc = cmac(acc, h, x[j - 1]);
+                    dacc = cmac(dacc, h, dx[j - 1]);
+                }
+                const cx<float> sub = Hf.ld(i, i - 1);
+                if (sub.r == 0.f && sub.i == 0.f) { ok = false; break; }
+                x[i - 2] = cdiv(mk(-acc.r, -acc.i), sub);
+                dx[i - 2] = cdiv(mk(-dacc.r, -dacc.i), sub);
+                if (cabs1(x[i - 2]) > 1e18f) {
+                    for (int j = i - 1; j <= n; ++j) { x[j - 1] = cscal(x[j - 1], 1e-18f); dx[j - 1] = cscal(dx[j - 1], 1e-18f); }
+                }
+            }
+            if (!ok) break;
+            const cx<float> d1 = csub(Hf.ld(1, 1), s);
+            cx<float> r = cmul(d1, x[0]);
+            cx<float> rp = csub(cmul(d1, dx[0]), x[0]);
+            for (int j = 2; j <= n; ++j) {
+                const cx<float> h = Hf.ld(1, j);
+                r = cmac(r, h, x[j - 1]);
+                rp = cmac(rp, h, dx[j - 1]);
+            }
+            const cx<float> delta = cdiv(r, rp);
+            if (nonfinite(delta.r) || nonfinite(delta.i)) { ok = false; break; }
+            s = csub(s, delta);
+            last = cabs1(delta);
+            if (last <= tol) break;
+        }
+        S.st(k, ok && last <= keep ? mk((double)s.r, (double)s.i) : mk(nan, nan));
+    }
+    for (int k = 2; k <= n; ++k) {
+        const cx<double> sk = S.ld(k);
+        for (int j = 1; j < k; ++j) {
+            const cx<double> sj = S.ld(j);
+            if (sj.r == sj.r && fabs(sj.r - sk.r) + fabs(sj.i - sk.i) <= (double)dup) {
+                S.st(k, mk(nan, nan));
+                break;
+            }
+        }
+    }
+}
 
 template <class R, bool kSchur = true, class MH, class MZ, class SP = NoShiftPredictions>
 __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool valid, const int max_its,
@@ -511,13 +600,25 @@ __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool va
             const R t2 = t1.r * w1.r - t1.i * w1.i;
             if (kSchur) {
                 if (act) {
-                    // rows K, K+1, columns K..n (wantT: I2 = n)
-                    const cx<R> c1 = conj(t1);
-                    for (int j = K; j <= n; ++j) {
-                        cx<R> h1 = H.ld(K, j), h2 = H.ld(K + 1, j);
-                        rot_pair(h1, h2, c1, t2, w1);
-                        H.st(K, j, h1);
-                        H.st(K + 1, j, h2);
+                    // rows K, K+1 of H (columns K..n; wantT: I2 = n) and columns
+                    // K, K+1 of Z (rows 1..n) in one loop: the two updates touch
+                    // disjoint data, and interleaving them gives every iteration two
+                    // independent rotation chains (the FP64 pipe's latency is hidden
+                    // by 2 warps per scheduler otherwise).  Same arithmetic per element.
+                    const cx<R> c1 = conj(t1), cw = conj(w1);
+                    for (int j = 1; j <= n; ++j) {
+                        cx<R> z1 = Z.ld(j, K), z2 = Z.ld(j, K + 1);
+                        if (j >= K) {
+                            cx<R> h1 = H.ld(K, j), h2 = H.ld(K + 1, j);
+                            rot_pair(z1, z2, t1, t2, cw);
+                            rot_pair(h1, h2, c1, t2, w1);
+                            H.st(K, j, h1);
+                            H.st(K + 1, j, h2);
+                        } else {
+                            rot_pair(z1, z2, t1, t2, cw);
+                        }
+                        Z.st(j, K, z1);
+                        Z.st(j, K + 1, z2);
                     }
                 }
             } else {
@@ -532,24 +633,28 @@ __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool va
                     }
                 }
             }
-            // columns K, K+1, rows I1..min(K+2, I) (I1 = 1, or L without the Schur form)
+            // columns K, K+1, rows I1..min(K+2, I) (I1 = 1, or L without the Schur
+            // form), after the row update (they share the 2x2 block at K, K+1);
+            // two rows per iteration for two independent chains
             const int je = (K + 2) < n ? (K + 2) : n;
-            for (int j = kSchur ? 1 : Kmin; j <= je; ++j) {
-                if (act && j <= I && (kSchur || j >= L)) {
-                    cx<R> h1 = H.ld(j, K), h2 = H.ld(j, K + 1);
-                    rot_pair(h1, h2, t1, t2, conj(w1));
-                    H.st(j, K, h1);
-                    H.st(j, K + 1, h2);
-                }
+            const cx<R> cw1 = conj(w1);
+            int j = kSchur ? 1 : Kmin;
+            for (; j + 1 <= je; j += 2) {
+                const bool pa = act && j <= I && (kSchur || j >= L);
+                const bool pb = act && j + 1 <= I && (kSchur || j + 1 >= L);
+                cx<R> a1 = mk(R(0), R(0)), a2 = a1, b1 = a1, b2 = a1;
+                if (pa) { a1 = H.ld(j, K); a2 = H.ld(j, K + 1); }
+                if (pb) { b1 = H.ld(j + 1, K); b2 = H.ld(j + 1, K + 1); }
+                rot_pair(a1, a2, t1, t2, cw1);
+                rot_pair(b1, b2, t1, t2, cw1);
+                if (pa) { H.st(j, K, a1); H.st(j, K + 1, a2); }
+                if (pb) { H.st(j + 1, K, b1); H.st(j + 1, K + 1, b2); }
             }
-            if (kSchur && act) {
-                const cx<R> cw = conj(w1);
-                for (int j = 1; j <= n; ++j) {
-                    cx<R> z1 = Z.ld(j, K), z2 = Z.ld(j, K + 1);
-                    rot_pair(z1, z2, t1, t2, cw);
-                    Z.st(j, K, z1);
-                    Z.st(j, K + 1, z2);
-                }
+            if (j <= je && act && j <= I && (kSchur || j >= L)) {
+                cx<R> h1 = H.ld(j, K), h2 = H.ld(j, K + 1);
+                rot_pair(h1, h2, t1, t2, cw1);
+                H.st(j, K, h1);
+                H.st(j, K + 1, h2);
             }
         }
         if (sweep) {
@@ -671,16 +776,6 @@ __device__ void backsubs_lane(const int n, const M &T, const V &x)
         x.st(j, xj);
         for (int i = j - 1; i >= 1; --i) x.st(i, csub(x.ld(i), cmul(T.ld(i, j), xj)));
     }
-}
-
-// Bit test for Inf/NaN without touching the FP64 pipe.
-__device__ __forceinline__ bool nonfinite(double v)
-{
-    return (__double2hiint(v) & 0x7ff00000) == 0x7ff00000;
-}
-__device__ __forceinline__ bool nonfinite(float v)
-{
-    return (__float_as_uint(v) & 0x7f800000u) == 0x7f800000u;
 }
 
 }  // namespace ves

@@ -36,6 +36,7 @@ struct FusedArgs {
     const double *rS, *iS;
     int shift_sweeps;
     float shift_gate;  // predictions used only while |H(I,I-1)| > shift_gate * ||A||_F / sqrt(n)
+    int shift_polish;  // Newton steps on det(H - sI) per prediction (FP32) before the QR; 0 = none
     int *fallbacks;
     int blocks_per_sm;  // persistent grid: blocks (4 warps) per SM; 0 = default
 };
@@ -62,7 +63,10 @@ cudaError_t launch_mixed(const MixedArgs &a, cudaStream_t st);
 
 // Fused zgehrd -> zunghr -> zlahqr -> ztrevc, FP64.
 // blocks_per_sm = 0 takes the library default (VES_FUSED_BLOCKS_PER_SM, else 2).
-size_t fused_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blocks, int *out_threads);
+// learned = the shift-seeded kernel, whose slots also hold an FP32 copy of H
+// and the n predictions.
+size_t fused_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blocks, int *out_threads,
+                             bool learned = false);
 cudaError_t launch_fused_fp64(const FusedArgs &a, cudaStream_t st);
 
 // Stage kernels, in place on the SoA layout (reference call_* semantics).

@@ -25,6 +25,15 @@ namespace {
 
 constexpr int kFusedThreads = 128;  // 4 warps per block
 
+// double2 elements per lane of one fused-kernel slot: H, Z (n^2 each), a work
+// vector (n); the shift-seeded kernel adds an FP32 copy of H (n^2 float2 =
+// ceil(n^2 / 2) double2) and the n predictions.
+__host__ __device__ __forceinline__ long long fused_slot_elems(int n, bool learned)
+{
+    const long long nn = (long long)n * n;
+    return 2 * nn + n + (learned ? (nn + 1) / 2 + n : 0);
+}
+
 __device__ __forceinline__ long long soa_mat_off(long long m, int n, int tc)
 {
     return (m / tc) * (long long)tc * n * n + (m % tc);
@@ -65,7 +74,7 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
     const long long nslots = (long long)gridDim.x * (kFusedThreads / 32);
     const long long Nw = a.list ? (long long)*a.list_count : N;
     const long long ngroups = (Nw + 31) / 32;
-    const long long per_lane = 2LL * n * n + n;  // H, Z, work vector
+    const long long per_lane = fused_slot_elems(n, kLearned);  // H, Z, work vector (+ FP32 H, predictions)
 
     double2 *base = reinterpret_cast<double2 *>(a.ws) + slot * per_lane * 32 + lane;
     const MatIlv<double> H{base, n};
@@ -98,9 +107,38 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
         }
         ShiftPredictions sp{};
         if (kLearned) {
-            sp.re = a.rS + vo;
-            sp.im = a.iS + vo;
-            sp.s = tc;
+            // predictions into the slot, optionally polished on H in FP32
+            const VecIlv<double> S{base + (2LL * n * n + n + ((long long)n * n + 1) / 2) * 32};
+            const double scale = sqrt(fro2 / (double)n);
+            if (valid) {
+                for (int k = 1; k <= n; ++k)
+                    S.st(k, mk(a.rS[vo + (long long)(k - 1) * tc], a.iS[vo + (long long)(k - 1) * tc]));
+            }
+            if (a.shift_polish > 0) {
+                // FP32 copy of the Hessenberg matrix: lane l's element e at float2
+                // index e * 32 + l of the region after H, Z and the work vector
+                float2 *region = reinterpret_cast<float2 *>(base - lane + (2LL * n * n + n) * 32);
+                const MatIlv<float> Hf{region + lane, n};
+                const bool go = valid && !(status & ST_NONFINITE);
+                if (go)
+                    for (int j = 1; j <= n; ++j)
+                        for (int i = 1; i <= (j + 1 < n ? j + 1 : n); ++i) {
+                            const cx<double> h = H.ld(i, j);
+                            Hf.st(i, j, mk((float)h.r, (float)h.i));
+                        }
+                // stop below 1e-6 of the eigenvalue scale (FP32 resolution); keep
+                // a prediction whose last step was below 1e-3 of it
+                const float tol = (float)(1e-6 * scale), keep = (float)(1e-3 * scale), dup = (float)(1e-5 * scale);
+                if (go) {
+                    if (n <= 16)
+                        polish_shifts_lane<16>(n, Hf, S, a.shift_polish, tol, keep, dup);
+                    else if (n <= 32)
+                        polish_shifts_lane<32>(n, Hf, S, a.shift_polish, tol, keep, dup);
+                    else
+                        polish_shifts_lane<64>(n, Hf, S, a.shift_polish, tol, keep, dup);
+                }
+            }
+            sp.S = S;
             sp.n = n;
             sp.sweeps = a.shift_sweeps;
             sp.gate = (double)a.shift_gate * sqrt(fro2 / (double)n);
@@ -251,7 +289,7 @@ int g_fused_blocks_per_sm = 2;  // 8 warps per SM; tunable through VES_FUSED_BLO
 
 }  // namespace
 
-size_t fused_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blocks, int *out_threads)
+size_t fused_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blocks, int *out_threads, bool learned)
 {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -270,7 +308,7 @@ size_t fused_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blo
     const int bps = blocks_per_sm > 0 ? blocks_per_sm : g_fused_blocks_per_sm;
     long long blocks = std::min<long long>((groups + wpb - 1) / wpb, (long long)sms * bps);
     if (blocks < 1) blocks = 1;
-    const size_t per_slot = (size_t)(2LL * n * n + n) * 32 * sizeof(double2);
+    const size_t per_slot = (size_t)fused_slot_elems(n, learned) * 32 * sizeof(double2);
     if (out_blocks) *out_blocks = (int)blocks;
     if (out_threads) *out_threads = kFusedThreads;
     return per_slot * (size_t)blocks * wpb;
@@ -280,7 +318,7 @@ cudaError_t launch_fused_fp64(const FusedArgs &a, cudaStream_t st)
 {
     if (a.g.N <= 0) return cudaSuccess;
     int blocks = 0, threads = 0;
-    fused_workspace_bytes(a.g.n, a.g.N, a.blocks_per_sm, &blocks, &threads);
+    fused_workspace_bytes(a.g.n, a.g.N, a.blocks_per_sm, &blocks, &threads, a.rS != nullptr);
     if (a.rS)
         fused_fp64_kernel<true><<<blocks, threads, 0, st>>>(a);
     else

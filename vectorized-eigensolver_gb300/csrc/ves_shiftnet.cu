@@ -37,6 +37,38 @@
 
 namespace ves {
 
+namespace {
+
+template <int NT>
+cudaError_t launch_persistent(int M, int N, int K, const __nv_bfloat16 *a, int lda, const __nv_bfloat16 *b, int ldb,
+                              const float *bias, int act, __nv_bfloat16 *c, float *cf, int ldc, int *err,
+                              cudaStream_t st)
+{
+    static int max_smem_set = -1, sms = 0;  // per process: one device's attributes (the GB300's)
+    const int smem = (tc::kM + NT) * K * 2;
+    if (max_smem_set < 0) {
+        const int cap = (tc::kM + NT) * 256 * 2;
+        cudaError_t e = cudaFuncSetAttribute(tc::gemm_bf16_persistent_kernel<NT>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+        if (e != cudaSuccess) return e;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        max_smem_set = cap;
+    }
+    constexpr int kCols = NT <= 32 ? 32 : (NT <= 64 ? 64 : (NT <= 128 ? 128 : 256));
+    const int per_sm = std::max(1, std::min(512 / kCols, (220 * 1024) / smem));
+    const int mtiles = (M + tc::kM - 1) / tc::kM;
+    const unsigned gx = (unsigned)std::max(1, std::min(mtiles, std::max(sms, 1) * per_sm));
+    tc::gemm_bf16_persistent_kernel<NT><<<dim3(gx, (N + NT - 1) / NT), 128, smem, st>>>(a, lda, b, ldb, M, N, K, bias,
+                                                                                      act, c, cf, ldc, err);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// The persistent kernel when K <= 256 and the shapes allow 16-byte vector
+// stores; the K-chunked kernel otherwise.
 cudaError_t launch_gemm_bf16(int M, int N, int K, const void *A, int lda, const void *Bt, int ldb, const float *bias,
                              int act, void *C, float *Cf, int ldc, int *err, cudaStream_t st)
 {
@@ -44,6 +76,12 @@ cudaError_t launch_gemm_bf16(int M, int N, int K, const void *A, int lda, const 
     const auto *a = static_cast<const __nv_bfloat16 *>(A);
     const auto *b = static_cast<const __nv_bfloat16 *>(Bt);
     auto *c = static_cast<__nv_bfloat16 *>(C);
+    const bool vec_ok = (N % 16) == 0 && (ldc % 8) == 0 && ((uintptr_t)C & 15) == 0 && ((uintptr_t)Cf & 15) == 0;
+    if (K % 16 == 0 && K <= 256 && vec_ok) {
+        if (N > 128) return launch_persistent<256>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
+        if (N > 64) return launch_persistent<128>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
+        return launch_persistent<64>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
+    }
     const unsigned gx = (unsigned)((M + tc::kM - 1) / tc::kM);
     if (N > 64) {
         tc::gemm_bf16_kernel<256><<<dim3(gx, (N + 255) / 256), 128, 0, st>>>(a, lda, b, ldb, M, N, K, bias, act, c,
@@ -311,17 +349,30 @@ __global__ void gelu_f32_kernel(long long total, const float *Z, float *Hf)
 }
 
 // Output layer in FP32 on CUDA cores (no BF16 rounding of the last hidden
-// activations or of the output weights): Y[r][o] = b[o] + sum_i W[o][i] Hf[r][i],
-// one thread per (r, o).
-__global__ void dense_out_kernel(int rows, int out, int in, const float *Hf, const float *W, const float *b, float *Y)
+// activations or of the output weights): Y[r][o] = b[o] + sum_i W[o][i]
+// GELU(Z[r][i]).  A block of 128 threads takes 32 rows: the rows' activations
+// are staged in shared memory (coalesced reads, GELU applied once), then lane
+// l of warp w computes row l for outputs w, w + 4, ... (the W row is a
+// broadcast read).
+constexpr int kOutRows = 32;
+__global__ void __launch_bounds__(128) dense_out_kernel(int rows, int out, int in, const float *Z, const float *W,
+                                                        const float *b, float *Y)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)rows * out) return;
-    const int r = (int)(t / out), o = (int)(t % out);
-    const float *h = Hf + (long long)r * in, *w = W + (long long)o * in;
-    float acc = b[o];
-    for (int i = 0; i < in; ++i) acc = fmaf(w[i], h[i], acc);
-    Y[t] = acc;
+    extern __shared__ float hs[];  // [kOutRows][in + 1]
+    const int r0 = blockIdx.x * kOutRows, ld = in + 1;
+    for (int e = threadIdx.x; e < kOutRows * in; e += blockDim.x) {
+        const int r = e / in, i = e % in;
+        hs[r * ld + i] = r0 + r < rows ? tc::gelu(Z[(long long)(r0 + r) * in + i]) : 0.f;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int r = r0 + lane;
+    for (int o = warp; o < out; o += 4) {
+        const float *w = W + (long long)o * in;
+        float acc = b[o];
+        for (int i = 0; i < in; ++i) acc = fmaf(w[i], hs[lane * ld + i], acc);
+        if (r < rows) Y[(long long)r * out + o] = acc;
+    }
 }
 
 // dH[b][i] = sum_o dZ[b][o] * W[o][i]
@@ -476,22 +527,29 @@ Acts carve_acts(const ves_shiftnet *t, size_t rows, char *&w)
     return a;
 }
 
-// forward over `rows` rows of X (BF16 [rows x kin_pad])
-cudaError_t forward(const ves_shiftnet *t, int rows, const ves::bf16 *X, const Acts &a, int *err, cudaStream_t st)
+// forward over `rows` rows of X (BF16 [rows x kin_pad]); training keeps every
+// hidden layer's FP32 pre-activation for the backward pass, inference only the
+// last one (the FP32 output layer's input)
+cudaError_t forward(const ves_shiftnet *t, int rows, const ves::bf16 *X, const Acts &a, int *err, cudaStream_t st,
+                    bool training)
 {
     const void *in = X;
     int ld = t->kin_pad;
     for (int l = 0; l < t->L; ++l) {
+        float *zf = (training || l == t->L - 1) ? a.Z[l] : nullptr;
         cudaError_t e = ves::launch_gemm_bf16(rows, t->H, t->in[l], in, ld, t->Wb[l], t->in[l], t->b[l], 1, a.Hs[l],
-                                              a.Z[l], t->H, err, st);
+                                              zf, t->H, err, st);
         if (e != cudaSuccess) return e;
         in = a.Hs[l];
         ld = t->H;
     }
-    const long long nh = (long long)rows * t->H;
-    ves::gelu_f32_kernel<<<ves::nb(nh), 256, 0, st>>>(nh, a.Z[t->L - 1], a.Hf);
-    const long long no = (long long)rows * t->nout_pad;
-    ves::dense_out_kernel<<<ves::nb(no), 256, 0, st>>>(rows, t->nout_pad, t->H, a.Hf, t->W[t->L], t->b[t->L], a.Y);
+    if (training) {  // FP32 activations of the last hidden layer, for the output layer's weight gradient
+        const long long nh = (long long)rows * t->H;
+        ves::gelu_f32_kernel<<<ves::nb(nh), 256, 0, st>>>(nh, a.Z[t->L - 1], a.Hf);
+    }
+    const size_t smem = (size_t)ves::kOutRows * (t->H + 1) * sizeof(float);
+    ves::dense_out_kernel<<<ves::nb(rows, ves::kOutRows), 128, smem, st>>>(rows, t->nout_pad, t->H, a.Z[t->L - 1],
+                                                                         t->W[t->L], t->b[t->L], a.Y);
     return cudaGetLastError();
 }
 
@@ -629,7 +687,7 @@ int ves_shiftnet_train(ves_shiftnet *t, long long count, int thread_cnt, const d
                                                                      iA, t->fmean, t->fstd, t->kin, t->kin_pad, Xb, r);
                 ves::targets_kernel<<<ves::nb(batch), 256, 0, st>>>(batch, n, thread_cnt, rE, iE, t->tmean, t->tstd,
                                                                     t->nout_pad, Tb, r);
-                forward(t, batch, Xb, a, err, st);
+                forward(t, batch, Xb, a, err, st, true);
                 ves::chamfer_kernel<<<ves::nb(batch, 128), 128, 0, st>>>(batch, n, t->nout_pad, a.Y, Tb, dA, loss,
                                                                          t->cfg.loss, t->cfg.delta);
                 // output layer (FP32): dW = dY^T Hf, dH = dY W, then through GELU
@@ -705,7 +763,7 @@ int ves_shiftnet_predict(const ves_shiftnet *t, long long count, int thread_cnt,
     int *err = nullptr;  // a GEMM wait that gives up leaves its tile unwritten; training checks the flag
     ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, t->n, t->P, t->F, thread_cnt, params, rA, iA,
                                                          t->fmean, t->fstd, t->kin, t->kin_pad, X, nullptr);
-    if (forward(t, (int)count, X, a, err, st) != cudaSuccess) return VES_ERR_CUDA;
+    if (forward(t, (int)count, X, a, err, st, false) != cudaSuccess) return VES_ERR_CUDA;
     ves::shifts_out_kernel<<<ves::nb(count), 256, 0, st>>>(count, t->n, thread_cnt, t->nout_pad, a.Y, t->tmean,
                                                            t->tstd, rS, iS);
     return cudaGetLastError() == cudaSuccess ? VES_OK : VES_ERR_CUDA;

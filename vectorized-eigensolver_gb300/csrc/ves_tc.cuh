@@ -210,5 +210,144 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *A, 
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols));
 }
 
+// ---------------------------------------------------------------------------
+// Persistent variant for K <= 256 (the network's layers): the CTA keeps the
+// whole N-tile of B (the weights, NT x K) in shared memory for all its M-tiles
+// and stages each 128 x K A-tile whole, so one tcgen05.commit covers the K/16
+// MMAs of a tile.  The A-tile of the CTA's next M-tile is fetched with cp.async
+// while the epilogue of the current one drains TMEM; the epilogue stores 16
+// consecutive columns per thread as 16-byte vectors.  Dynamic shared memory:
+// (128 + NT) * K * 2 bytes (192 KB at K = 256, NT = 256).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async16(uint32_t saddr, const void *g, uint32_t src_bytes)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(saddr), "l"(g), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+// rows x K (K-major) from global into the no-swizzle core-matrix layout;
+// rows past `valid` are zero-filled
+__device__ __forceinline__ void stage_rows(unsigned char *dst, const __nv_bfloat16 *src, int ld, int rows, int valid,
+                                           int K)
+{
+    const int kcs = K / 8;  // 16-byte core-matrix columns
+    const uint32_t base = smem_addr(dst);
+    for (int p = threadIdx.x; p < rows * kcs; p += blockDim.x) {
+        const int r = p / kcs, kc = p % kcs;
+        const bool ok = r < valid;
+        const __nv_bfloat16 *g = ok ? src + (size_t)r * ld + kc * 8 : src;
+        cp_async16(base + (uint32_t)(((r >> 3) * kcs + kc) * 128 + (r & 7) * 16), g, ok ? 16u : 0u);
+    }
+}
+
+template <int NT>
+__global__ void __launch_bounds__(128) gemm_bf16_persistent_kernel(const __nv_bfloat16 *A, int lda,
+                                                                   const __nv_bfloat16 *Bt, int ldb, int M, int N,
+                                                                   int K, const float *bias, int act,
+                                                                   __nv_bfloat16 *C, float *Cf, int ldc, int *err)
+{
+    static_assert(NT % 16 == 0 && NT >= 16 && NT <= 256, "N tile");
+    constexpr int kCols = NT <= 32 ? 32 : (NT <= 64 ? 64 : (NT <= 128 ? 128 : 256));
+    extern __shared__ __align__(1024) unsigned char dsm[];
+    unsigned char *sA = dsm;
+    unsigned char *sB = dsm + (size_t)kM * K * 2;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int failed;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int n0 = blockIdx.y * NT;
+    const int mtiles = (M + kM - 1) / kM;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
+                     "r"(kCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        failed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    int tile = blockIdx.x;
+    // B (this CTA's N-tile, all of K) and the first A-tile
+    stage_rows(sB, Bt + (size_t)n0 * ldb, ldb, NT, N - n0, K);
+    if (tile < mtiles) stage_rows(sA, A + (size_t)tile * kM * lda, lda, kM, M - tile * kM, K);
+    cp_async_wait_all();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_base;
+    constexpr uint32_t idesc = make_idesc(kM, NT);
+    const uint32_t sbo = (uint32_t)(K / 8) * 128;
+
+    unsigned phase = 0;
+    for (; tile < mtiles && !failed; tile += gridDim.x) {
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            for (int s = 0; s < K / 16; ++s) {
+                const uint64_t da = make_desc(smem_addr(sA) + s * 256, 128, sbo);
+                const uint64_t db = make_desc(smem_addr(sB) + s * 256, 128, sbo);
+                mma_bf16(tmem, da, db, idesc, s > 0 ? 1u : 0u);
+            }
+            mma_commit(&bar);
+        }
+        const bool ok = mbar_wait(&bar, phase);
+        phase ^= 1;
+        if (!ok) failed = 1;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        __syncthreads();  // every thread saw the MMAs complete (or the failure)
+        if (failed) break;
+        // the MMAs have read sA: fetch the next tile's A while draining TMEM
+        const int next = tile + gridDim.x;
+        if (next < mtiles) stage_rows(sA, A + (size_t)next * kM * lda, lda, kM, M - next * kM, K);
+        const int row = tile * kM + warp * 32 + lane;
+        for (int cb = 0; cb < NT; cb += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb, v);
+            const int col = n0 + cb;
+            if (row < M && col < N) {  // N is a multiple of 16: a chunk is all in or all out
+#pragma unroll
+                for (int i = 0; i < 16; ++i) v[i] += bias ? bias[col + i] : 0.f;
+                if (Cf) {
+                    float4 *dst = reinterpret_cast<float4 *>(Cf + (size_t)row * ldc + col);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                }
+                if (C) {
+                    uint32_t pk[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const float x0 = act == 1 ? gelu(v[2 * q]) : v[2 * q];
+                        const float x1 = act == 1 ? gelu(v[2 * q + 1]) : v[2 * q + 1];
+                        __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+                        pk[q] = *reinterpret_cast<uint32_t *>(&h);
+                    }
+                    uint4 *dst = reinterpret_cast<uint4 *>(C + (size_t)row * ldc + col);
+                    dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                    dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                }
+            }
+        }
+        cp_async_wait_all();
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();  // next A staged, TMEM drained
+    }
+    if (failed) {
+        // a wait gave up: give in-flight MMAs one more bounded wait, report, free TMEM
+        if (tid == 0) (void)mbar_wait(&bar, phase ^ 1);
+        if (tid == 0 && err) atomicExch(err, 1);
+        cp_async_wait_all();
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols));
+}
+
 }  // namespace tc
 }  // namespace ves

@@ -45,7 +45,7 @@ VES_SHIFTNET_LOSS_CHAMFER, VES_SHIFTNET_LOSS_ROBUST = 0, 1
 class Options(ctypes.Structure):
     _fields_ = [("precision", _int), ("max_its", _int), ("vnorm", _int), ("refine_steps", _int),
                 ("refine_tol", _dbl), ("want_vectors", _int), ("blocks_per_sm", _int), ("varsize_order", _int),
-                ("shift_sweeps", _int), ("shift_gate", ctypes.c_float), ("reserved", _int)]
+                ("shift_sweeps", _int), ("shift_gate", ctypes.c_float), ("shift_polish", _int)]
 
 
 # exported symbol -> (restype, argtypes); every name declared in include/ves.h
