@@ -289,17 +289,24 @@ def eig_distance(E1, E0, A, chunk=1 << 17):
     return worst
 
 
+LEARNED_NET = dict(hidden=256, layers=4, fourier=8, loss=1, delta=0.01)  # ves_shiftnet_config
+LEARNED_EPOCHS = 150
+LEARNED_POLISH = 6     # Newton steps per prediction (FP32, on the Hessenberg form)
+LEARNED_GATE = 3e-2    # predictions only while |H(I,I-1)| > gate * ||A||_F / sqrt(n)
+
+
 def measure_learned(n, N, train_count, epochs, steps, tc=512):
     """The learned-shift form on the parametric family A(p) = A0 + p1 A1 + p2 A2
     + p3 A3 (order n): the network is trained (tcgen05 BF16 MLP) on
     `train_count` plain-solver solutions (param seed 5), then on a fresh batch
-    (param seed 6) one step = network inference + shift-seeded FP64 solve,
-    against the plain FP64 solve of the same batch."""
+    (param seed 6) one step = network inference + the shift-seeded FP64 solve
+    (predictions polished by Newton steps, gated), against the plain FP64 solve
+    of the same batch."""
     import torch
     import ves
     import learned_shift
     t0 = time.perf_counter()
-    net, losses = learned_shift.train(n, count=train_count, epochs=epochs, batch=1024, lr=1e-3, hidden=256)
+    net, losses = learned_shift.train(n, count=train_count, epochs=epochs, batch=1024, lr=1e-3, **LEARNED_NET)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     p, rA, iA = learned_shift.family(N, n, param_seed=6, thread_cnt=tc)
@@ -310,6 +317,8 @@ def measure_learned(n, N, train_count, epochs, steps, tc=512):
     rV, iV = torch.empty_like(rA), torch.empty_like(iA)
     sw0, sw, st, fb = (torch.zeros(N, dtype=torch.int32, device="cuda") for _ in range(4))
     ws = ves.Workspace(n, bc, tc)
+    lopt = ves.default_options(shift_polish=LEARNED_POLISH, shift_gate=LEARNED_GATE)
+    lws = ves.shifts_workspace(n, bc, tc, lopt)
     pws = net.predict_workspace(N)
     stream = torch.cuda.current_stream()
 
@@ -318,7 +327,8 @@ def measure_learned(n, N, train_count, epochs, steps, tc=512):
 
     def learned(**kw):
         net.predict_into(N, tc, p, rA, iA, rS, iS, pws, stream=stream)
-        ves.eigensolve_shifts(n, bc, tc, rA, iA, rE, iE, rV, iV, rS, iS, workspace=ws, stream=stream, **kw)
+        ves.eigensolve_shifts(n, bc, tc, rA, iA, rE, iE, rV, iV, rS, iS, options=lopt, workspace=lws,
+                              stream=stream, **kw)
 
     def timed(fn):
         for _ in range(2):
@@ -351,10 +361,11 @@ def measure_learned(n, N, train_count, epochs, steps, tc=512):
            "fallback_per_eigenvalue": float(fb.double().mean()) / n,
            "prediction_error_median_rel": float((pred_err / nA[:, None]).median()),
            "train": {"matrices": train_count, "epochs": epochs, "seconds": train_s, "loss_first": losses[0],
-                     "loss_last": losses[-1]},
+                     "loss_last": losses[-1], "network": LEARNED_NET},
+           "shift_polish": LEARNED_POLISH, "shift_gate": LEARNED_GATE,
            "max_residual": ver["max_residual"], "nonfinite": ver["nonfinite"], "max_eig_err_rel": err,
            "passed": ver["max_residual"] <= RES_TOL and ver["nonfinite"] == 0 and err <= 1e-12 and other == 0}
-    del net, rA, iA, rV, iV, ws, pws, A
+    del net, rA, iA, rV, iV, ws, lws, pws, A
     torch.cuda.empty_cache()
     return out
 
@@ -542,7 +553,7 @@ def run_gpu_arm(args, d):
         forms += [p32, m32]
         for ln in (16, 32):
             log("[bench] learned-shift form, n=%d" % ln)
-            forms.append(measure_learned(ln, 262_144, 200_000, 20, 2))
+            forms.append(measure_learned(ln, 262_144, 200_000, LEARNED_EPOCHS, 2))
         log("[bench] mixed-size form")
         forms.append(measure_varsize(500_000, 2))
 

@@ -132,7 +132,9 @@ typedef struct ves_options {
                         * |H(I,I-1)| exceeds shift_gate * ||A||_F / sqrt(n) (below that the Wilkinson shift
                         * is the better estimate); set it to the predictor's typical error; default 0 */
     int shift_polish;  /* ves_eigensolve_shifts: Newton steps on det(H - sI) (FP32, Hyman's recurrence on the
-                        * Hessenberg matrix) that refine each prediction before the QR; 0 (default) = none */
+                        * Hessenberg matrix) that refine each prediction before the QR; a prediction that does
+                        * not converge or lands on an eigenvalue already seeded is dropped; for dim <= 32 this
+                        * runs as a warp-per-matrix pre-pass; 0 (default) = none */
 } ves_options;
 
 void ves_default_options(ves_options *opt);
@@ -200,6 +202,7 @@ void ves_graph_destroy(ves_graph *graph);
  * results carry the same backward-error guarantee.  fallbacks (nullable) gets
  * per matrix the number of eigenvalues that needed more than shift_sweeps + 2
  * sweeps (VES_STATUS_SHIFT_FALLBACK marks those matrices). */
+size_t ves_eigensolve_shifts_workspace_size(int dim, int block_cnt, int thread_cnt, const ves_options *opt);
 int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt,
                           const double *rA, const double *iA, double *rE, double *iE, double *rV, double *iV,
                           const double *rS, const double *iS, int *status, int *sweeps, int *fallbacks,

@@ -93,3 +93,41 @@ def test_gate_closed_equals_plain_solver():
     rE, iE, st, sw, fb, res = solve_shifts(n, N, rA, iA, far, torch.zeros_like(far), shift_gate=1e6)
     assert torch.equal(rE, rE0) and torch.equal(iE, iE0) and torch.equal(sw, sw0)
     assert fb.sum().item() == 0 and (st == 0).all()
+
+
+@pytest.mark.parametrize("n", [16, 40])
+def test_polish_far_predictions_dropped(n):
+    """Predictions far from the spectrum do not converge in a few Newton
+    steps and are dropped: the solve is then the plain solver, bit for bit
+    (n = 16 runs the warp pre-pass, n = 40 the in-kernel polish)."""
+    import torch
+    N = 2048
+    p, rA, iA = learned_shift.family(N, n, param_seed=13)
+    rE0, iE0, sw0 = learned_shift.solve_plain(n, N, rA, iA, TC, vectors=True)
+    far = torch.full_like(rE0, 100.0)
+    rE, iE, st, sw, fb, res = solve_shifts(n, N, rA, iA, far, torch.zeros_like(far), shift_polish=4)
+    assert torch.equal(rE, rE0) and torch.equal(iE, iE0) and torch.equal(sw, sw0)
+    assert fb.sum().item() == 0
+
+
+@pytest.mark.parametrize("n", [16, 32, 40])
+def test_polish_recovers_noisy_predictions(n):
+    """Eigenvalues with 1% noise as predictions: the Newton polish brings them
+    back to FP32 accuracy, the QR needs clearly fewer sweeps, the result meets
+    the plain solver's bar."""
+    import torch
+    N = 4096
+    p, rA, iA = learned_shift.family(N, n, param_seed=14)
+    rE0, iE0, sw0 = learned_shift.solve_plain(n, N, rA, iA, TC)
+    g = torch.Generator(device="cuda").manual_seed(1)
+    rS = rE0 + 1e-2 * torch.randn(rE0.shape, generator=g, device="cuda", dtype=torch.float64)
+    iS = iE0 + 1e-2 * torch.randn(rE0.shape, generator=g, device="cuda", dtype=torch.float64)
+    rE, iE, st, sw, fb, res = solve_shifts(n, N, rA, iA, rS, iS, shift_polish=4)
+    assert res <= 1e-13
+    E0 = ves.complex_vec_from_soa(rE0.cpu().numpy(), iE0.cpu().numpy(), n, TC)
+    E = ves.complex_vec_from_soa(rE.cpu().numpy(), iE.cpu().numpy(), n, TC)
+    nA = np.linalg.norm(ves.complex_from_soa(rA.cpu().numpy(), iA.cpu().numpy(), n, TC), axis=(1, 2))
+    _, err, _ = match_eigs(E, E0)
+    assert (err / nA).max() <= 1e-12
+    assert sw.double().mean().item() < 0.8 * sw0.double().mean().item()
+    assert ((st & ~ves.VES_STATUS_SHIFT_FALLBACK) == 0).all()

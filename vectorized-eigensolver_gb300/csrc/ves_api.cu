@@ -676,6 +676,31 @@ int ves_complex_from_soa_vec(int dim, int block_cnt, int thread_cnt, const doubl
     return transpose_call(false, true, dim, block_cnt, thread_cnt, re, im, nullptr, nullptr, nullptr, z, 0, stream);
 }
 
+// Workspace of ves_eigensolve_shifts: the shift-seeded kernel's slots, and
+// for the polish pre-pass (shift_polish > 0, dim <= 32) the polished
+// predictions (two SoA vector planes).
+struct ShiftsPlan {
+    size_t fused, polish, total;
+};
+ShiftsPlan shifts_plan(int dim, long long N, const ves_options &o)
+{
+    ShiftsPlan p{};
+    p.fused = align256(ves::fused_workspace_bytes(dim, N, o.blocks_per_sm, nullptr, nullptr, true));
+    p.polish = (o.shift_polish > 0 && dim <= 32) ? align256((size_t)N * dim * 2 * sizeof(double)) : 0;
+    p.total = p.fused + p.polish;
+    return p;
+}
+
+size_t ves_eigensolve_shifts_workspace_size(int dim, int block_cnt, int thread_cnt, const ves_options *opt)
+{
+    ves::Geom g;
+    if (!geom_ok(dim, block_cnt, thread_cnt, &g) || dim > 64) return 0;
+    ves_options o;
+    ves_default_options(&o);
+    if (opt) o = *opt;
+    return shifts_plan(dim, g.N, o).total;
+}
+
 int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *rA, const double *iA, double *rE,
                           double *iE, double *rV, double *iV, const double *rS, const double *iS, int *status,
                           int *sweeps, int *fallbacks, const ves_options *opt, void *workspace,
@@ -696,7 +721,8 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *
         set_error("option out of range");
         return VES_ERR_ARG;
     }
-    const size_t need = align256(ves::fused_workspace_bytes(dim, g.N, o.blocks_per_sm, nullptr, nullptr, true));
+    const ShiftsPlan plan = shifts_plan(dim, g.N, o);
+    const size_t need = plan.total;
     void *ws = workspace;
     std::unique_lock<std::mutex> lk;
     if (!ws) {
@@ -720,7 +746,18 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *
     a.shift_polish = o.shift_polish;
     a.fallbacks = fallbacks;
     a.blocks_per_sm = o.blocks_per_sm;
-    return native(cuda_ok(ves::launch_fused_fp64(a, (cudaStream_t)stream), "learned-shift solve launch"));
+    cudaStream_t st = (cudaStream_t)stream;
+    if (plan.polish) {
+        // n <= 32: polish in a warp-per-matrix FP32 pre-pass, the solve reads the result
+        double *rP = reinterpret_cast<double *>(static_cast<char *>(ws) + plan.fused);
+        double *iP = rP + (size_t)g.N * dim;
+        if (!cuda_ok(ves::launch_polish32(g, rA, iA, rS, iS, rP, iP, o.shift_polish, st), "shift polish launch"))
+            return VES_ERR_CUDA;
+        a.rS = rP;
+        a.iS = iP;
+        a.shift_polish = 0;
+    }
+    return native(cuda_ok(ves::launch_fused_fp64(a, st), "learned-shift solve launch"));
 }
 
 int ves_gemm_bf16(int M, int N, int K, const void *A, int lda, const void *Bt, int ldb, const float *bias, int act,

@@ -412,6 +412,82 @@ __device__ __forceinline__ void zlarfg2(cx<R> &v0, cx<R> &v1, cx<R> &t1)
     v0 = mk(-beta, R(0));
 }
 
+// ---------------------------------------------------------------------------
+// Warp-cooperative FP32 helpers: one matrix per warp in shared memory
+// (column-major, leading dimension lda = n + 1 so that a row sweep and a
+// column sweep are both free of bank conflicts).  Lane l owns row l + 1 in
+// column operations and column l + 1 in row operations; scalar steps run
+// redundantly on all lanes from shared values (uniform control flow).
+// ---------------------------------------------------------------------------
+struct SmemMat {
+    float2 *p;
+    int lda;
+    __device__ __forceinline__ cx<float> ld(int i, int j) const
+    {
+        const float2 v = p[(i - 1) + (j - 1) * lda];
+        return mk(v.x, v.y);
+    }
+    __device__ __forceinline__ void st(int i, int j, cx<float> v) const { p[(i - 1) + (j - 1) * lda] = make_float2(v.r, v.i); }
+};
+struct SmemCol {  // column of a SmemMat as a vector
+    float2 *p;
+    __device__ __forceinline__ cx<float> ld(int i) const { const float2 v = p[i - 1]; return mk(v.x, v.y); }
+    __device__ __forceinline__ void st(int i, cx<float> v) const { p[i - 1] = make_float2(v.r, v.i); }
+};
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    return v;
+}
+
+// zgehd2 on the warp's matrix (n <= 32): H = Q^H A Q, the same reflector
+// conventions and per-element operation order as zgehrd_lane; reflector
+// vectors below the subdiagonal, tau(i) in sTau[i - 1].
+__device__ __forceinline__ void hess32_warp(const int n, const SmemMat &H, float2 *sTau, const int lane)
+{
+    const int j = lane + 1;
+    for (int i = 1; i <= n - 1; ++i) {
+        const int mm = n - i;
+        const cx<float> xk = (j >= i + 2 && j <= n) ? H.ld(j, i) : mk(0.f, 0.f);
+        const float xnorm2 = warp_sum(fmaf(xk.i, xk.i, xk.r * xk.r));
+        const cx<float> alpha = H.ld(i + 1, i);
+        const bool trivial = (xnorm2 == 0.f) && (alpha.i == 0.f);
+        const float beta = trivial ? alpha.r : -copysignf(sqrtf(alpha.r * alpha.r + alpha.i * alpha.i + xnorm2), alpha.r);
+        cx<float> t = mk(0.f, 0.f), scale = mk(0.f, 0.f);
+        if (!trivial) {
+            const float rb = 1.f / beta;
+            t = mk((beta - alpha.r) * rb, -alpha.i * rb);
+            scale = cinv(mk(alpha.r - beta, alpha.i));
+        }
+        __syncwarp();  // every lane has read alpha and its x element
+        if (j >= i + 2 && j <= n) H.st(j, i, cmul(xk, scale));
+        if (lane == 0) sTau[i - 1] = make_float2(t.r, t.i);
+        __syncwarp();
+        // right: row j of A(1:n, i+1:n) -= tau (A v)_j v^H
+        if (j <= n) {
+            cx<float> sacc = H.ld(j, i + 1);
+            for (int q = 2; q <= mm; ++q) sacc = cmac(sacc, H.ld(j, i + q), H.ld(i + q, i));
+            const cx<float> ts = cmul(t, sacc);
+            H.st(j, i + 1, csub(H.ld(j, i + 1), ts));
+            for (int q = 2; q <= mm; ++q) H.st(j, i + q, cnmacc(H.ld(j, i + q), ts, H.ld(i + q, i)));
+        }
+        __syncwarp();
+        // left: column j of A(i+1:n, i+1:n) -= conj(tau) v (v^H A)_j
+        if (j >= i + 1 && j <= n) {
+            const cx<float> tcj = conj(t);
+            cx<float> sacc = H.ld(i + 1, j);
+            for (int q = 2; q <= mm; ++q) sacc = cjmac(sacc, H.ld(i + q, i), H.ld(i + q, j));
+            const cx<float> ts = cmul(tcj, sacc);
+            H.st(i + 1, j, csub(H.ld(i + 1, j), ts));
+            for (int q = 2; q <= mm; ++q) H.st(i + q, j, cnmac(H.ld(i + q, j), H.ld(i + q, i), ts));
+        }
+        __syncwarp();
+        if (lane == 0) H.st(i + 1, i, mk(beta, 0.f));
+        __syncwarp();
+    }
+}
+
 //
 // kSchur = false is the eigenvalues-only form (LAPACK wantT = wantZ = false,
 // the reference's dead zlahqr_ at Toolbox.hpp:1663-1890): only the active block

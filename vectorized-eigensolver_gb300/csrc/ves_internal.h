@@ -86,6 +86,11 @@ cudaError_t launch_backsubs(Geom g, const double *rT, const double *iT, double *
 // workspace must hold blocks * 4 warp slots.
 cudaError_t launch_fused_fp64_blocks(const FusedArgs &a, int blocks, cudaStream_t st);
 
+// Learned-shift polish pre-pass (n <= 32): predictions (rS, iS) refined by
+// Newton steps on the FP32 Hessenberg form, written to (rP, iP); NaN = dropped.
+cudaError_t launch_polish32(Geom g, const double *rA, const double *iA, const double *rS, const double *iS,
+                            double *rP, double *iP, int steps, cudaStream_t st);
+
 // Eigenvalues only (no Q, no Schur vectors), companion-matrix roots, and the
 // SoA <-> interleaved-complex transposes.
 size_t eigvals_workspace_bytes(int n, long long N, int blocks_per_sm);

@@ -169,6 +169,138 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
 }
 
 // ---------------------------------------------------------------------------
+// Learned-shift polish pre-pass for n <= 32: one matrix per warp in shared
+// memory, FP32.  The warp reduces its matrix to Hessenberg form (hess32_warp;
+// FP32 rounding moves the eigenvalues by ~1e-7 relative, far below what the
+// shifts need), then lane k takes prediction k through up to `steps` Newton
+// steps on det(H - sI) by Hyman's recurrence (the iteration of
+// polish_shifts_lane, with every lane's x and x' in shared memory and H read
+// as broadcasts), keeping it only if its last step was below 1e-3 of the
+// eigenvalue scale ||A||_F / sqrt(n) and no lower lane landed within 1e-5 of
+// it; dropped predictions are NaN.  Output: rP, iP in the SoA vector layout.
+// ---------------------------------------------------------------------------
+constexpr int kPolishThreads = 128;  // 4 matrices per block
+
+__host__ __device__ __forceinline__ size_t polish_warp_elems(int n)
+{
+    return (size_t)n * (n + 1) + n + 2 * (size_t)n * 32;  // H, tau, x and x' of 32 lanes
+}
+
+__global__ void __launch_bounds__(kPolishThreads) polish32_warp_kernel(const Geom g, const double *rA,
+                                                                       const double *iA, const double *rS,
+                                                                       const double *iS, double *rP, double *iP,
+                                                                       int steps)
+{
+    extern __shared__ float2 psm[];
+    const int n = g.n, tc = g.tc;
+    const long long N = g.N;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int lda = n + 1;
+    float2 *sH = psm + (size_t)wib * polish_warp_elems(n);
+    float2 *sTau = sH + n * lda, *xs = sTau + n, *dxs = xs + n * 32;
+    const SmemMat H{sH, lda};
+    const long long nn = (long long)n * n;
+    const long long gw = (long long)blockIdx.x * (kPolishThreads / 32) + wib;
+    const long long nw = (long long)gridDim.x * (kPolishThreads / 32);
+    const float nanf_ = __int_as_float(0x7fc00000);
+    for (long long m = gw; m < N; m += nw) {
+        const long long mo = soa_mat_off(m, n, tc), vo = soa_vec_off(m, n, tc);
+        bool bad = false;
+        float s2 = 0.f;
+        for (int e = lane; e < nn; e += 32) {
+            const long long q = mo + (long long)e * tc;
+            const double re = rA[q], im = iA[q];
+            bad |= nonfinite(re) | nonfinite(im);
+            const float fr = (float)re, fi = (float)im;
+            s2 = fmaf(fi, fi, fmaf(fr, fr, s2));
+            sH[(e % n) + (e / n) * lda] = make_float2(fr, fi);
+        }
+        const float nA2 = warp_sum(s2);
+        const bool skip = __any_sync(FULL, bad) || !(nA2 < 1e36f) || n < 2;
+        cx<float> s = mk(0.f, 0.f);
+        if (lane < n) s = mk((float)rS[vo + (long long)lane * tc], (float)iS[vo + (long long)lane * tc]);
+        __syncwarp();
+        if (skip) {  // leave such matrices to the solver's own checks, predictions as given
+            if (lane < n) { rP[vo + (long long)lane * tc] = s.r; iP[vo + (long long)lane * tc] = s.i; }
+            continue;
+        }
+        hess32_warp(n, H, sTau, lane);
+        const float scale = sqrtf(nA2 / (float)n);
+        const float tol = 1e-6f * scale, keep = 1e-3f * scale, dup = 1e-5f * scale;
+        bool ok = lane < n && !nonfinite(s.r) && !nonfinite(s.i);
+        float last = 3.0e38f;
+        for (int it = 0; it < steps; ++it) {
+            const bool act = ok && last > tol;
+            if (!__any_sync(FULL, act)) break;
+            xs[(n - 1) * 32 + lane] = make_float2(1.f, 0.f);
+            dxs[(n - 1) * 32 + lane] = make_float2(0.f, 0.f);
+            bool broke = false;
+            for (int i = n; i >= 2; --i) {
+                const cx<float> d = csub(H.ld(i, i), s);
+                const float2 xi = xs[(i - 1) * 32 + lane], dxi = dxs[(i - 1) * 32 + lane];
+                cx<float> acc = cmul(d, mk(xi.x, xi.y));
+                cx<float> dacc = csub(cmul(d, mk(dxi.x, dxi.y)), mk(xi.x, xi.y));
+                for (int q = i + 1; q <= n; ++q) {
+                    const cx<float> h = H.ld(i, q);
+                    const float2 xq = xs[(q - 1) * 32 + lane], dxq = dxs[(q - 1) * 32 + lane];
+                    acc = cmac(acc, h, mk(xq.x, xq.y));
+                    dacc = cmac(dacc, h, mk(dxq.x, dxq.y));
+                }
+                const cx<float> sub = H.ld(i, i - 1);
+                if (sub.r == 0.f && sub.i == 0.f) { broke = true; break; }  // uniform: H is shared
+                cx<float> xn = cdiv(mk(-acc.r, -acc.i), sub), dxn = cdiv(mk(-dacc.r, -dacc.i), sub);
+                if (cabs1(xn) > 1e18f) {  // rescale x, x' together (the Newton ratio is scale free)
+                    for (int q = i; q <= n; ++q) {
+                        const float2 a0 = xs[(q - 1) * 32 + lane], a1 = dxs[(q - 1) * 32 + lane];
+                        xs[(q - 1) * 32 + lane] = make_float2(a0.x * 1e-18f, a0.y * 1e-18f);
+                        dxs[(q - 1) * 32 + lane] = make_float2(a1.x * 1e-18f, a1.y * 1e-18f);
+                    }
+                    xn = cscal(xn, 1e-18f);
+                    dxn = cscal(dxn, 1e-18f);
+                }
+                xs[(i - 2) * 32 + lane] = make_float2(xn.r, xn.i);
+                dxs[(i - 2) * 32 + lane] = make_float2(dxn.r, dxn.i);
+            }
+            if (broke) { ok = false; break; }
+            const cx<float> d1 = csub(H.ld(1, 1), s);
+            const float2 x1 = xs[lane], dx1 = dxs[lane];
+            cx<float> r = cmul(d1, mk(x1.x, x1.y));
+            cx<float> rp = csub(cmul(d1, mk(dx1.x, dx1.y)), mk(x1.x, x1.y));
+            for (int q = 2; q <= n; ++q) {
+                const cx<float> h = H.ld(1, q);
+                const float2 xq = xs[(q - 1) * 32 + lane], dxq = dxs[(q - 1) * 32 + lane];
+                r = cmac(r, h, mk(xq.x, xq.y));
+                rp = cmac(rp, h, mk(dxq.x, dxq.y));
+            }
+            if (act) {
+                const cx<float> delta = cdiv(r, rp);
+                if (nonfinite(delta.r) || nonfinite(delta.i)) {
+                    ok = false;
+                } else {
+                    s = csub(s, delta);
+                    last = cabs1(delta);
+                }
+            }
+        }
+        cx<float> res = ok && last <= keep ? s : mk(nanf_, nanf_);
+        // drop a prediction that a lower lane also converged to
+        bool dupl = false;
+        for (int q = 0; q < n; ++q) {
+            const float orr = __shfl_sync(FULL, res.r, q), oi = __shfl_sync(FULL, res.i, q);
+            if (q < lane && orr == orr && fabsf(orr - res.r) + fabsf(oi - res.i) <= dup) dupl = true;
+        }
+        if (dupl) res = mk(nanf_, nanf_);
+        if (lane < n) {
+            rP[vo + (long long)lane * tc] = res.r;
+            iP[vo + (long long)lane * tc] = res.i;
+        }
+        __syncwarp();
+    }
+}
+
+size_t polish_smem_bytes(int n) { return (kPolishThreads / 32) * polish_warp_elems(n) * sizeof(float2); }
+
+// ---------------------------------------------------------------------------
 // Stage kernels: one lane per matrix, in place on the SoA layout.
 // ---------------------------------------------------------------------------
 struct Lane {
@@ -323,6 +455,32 @@ cudaError_t launch_fused_fp64(const FusedArgs &a, cudaStream_t st)
         fused_fp64_kernel<true><<<blocks, threads, 0, st>>>(a);
     else
         fused_fp64_kernel<false><<<blocks, threads, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_polish32(Geom g, const double *rA, const double *iA, const double *rS, const double *iS,
+                            double *rP, double *iP, int steps, cudaStream_t st)
+{
+    if (g.N <= 0) return cudaSuccess;
+    if (g.n > 32) return cudaErrorInvalidValue;
+    static bool attr = false;
+    static int sms = 0;
+    if (!attr) {
+        cudaFuncSetAttribute(polish32_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)polish_smem_bytes(32));
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        attr = true;
+    }
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, polish32_warp_kernel, kPolishThreads,
+                                                  polish_smem_bytes(g.n));
+    const long long need = (g.N + kPolishThreads / 32 - 1) / (kPolishThreads / 32);
+    const long long blocks = std::max<long long>(1, std::min<long long>(need, (long long)std::max(sms, 1) *
+                                                                                   std::max(per_sm, 1)));
+    polish32_warp_kernel<<<(unsigned)blocks, kPolishThreads, polish_smem_bytes(g.n), st>>>(g, rA, iA, rS, iS, rP,
+                                                                                         iP, steps);
     return cudaGetLastError();
 }
 

@@ -38,6 +38,7 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 
 namespace ves {
 
@@ -131,9 +132,215 @@ __global__ void __launch_bounds__(kSchurThreads) schur32_kernel(const MixedArgs 
     }
 }
 
+// ---------------------------------------------------------------------------
+// schur32_warp_kernel: the same FP32 Schur stage for n <= 32 with one matrix
+// per warp.  H and Z live in shared memory (column-major, leading dimension
+// n + 1: a row sweep and a column sweep are both free of bank conflicts); lane
+// l owns row l + 1 in column operations and column l + 1 in row operations;
+// the scalar steps (reflectors, shifts, deflation tests) run redundantly on all
+// lanes from shared values, so control flow is uniform and no lane waits for
+// another matrix's sweeps, and H, Z never leave the SM.  Same algorithm and
+// operation order per element as the lane routines (zgehd2, zung2r, zlahqr
+// single shift, ztrevc back substitution); T, Z and the T-eigenvectors X go to
+// the per-matrix buffer layout read by refine_kernel.
+// ---------------------------------------------------------------------------
+constexpr int kWarpSchurThreads = 128;  // 4 matrices per block
+
+// per-matrix buffer layout: T, Z, X (n*n float2 each, column-major), then a
+// work vector whose first entry holds ||A||_F^2
+__host__ __device__ __forceinline__ long long mat_elems(int n) { return 3LL * n * n + n; }
+
+__host__ __device__ __forceinline__ size_t warp_schur_smem(int n)
+{
+    return (size_t)(kWarpSchurThreads / 32) * (2 * n * (n + 1) + n) * sizeof(float2);
+}
+
+__global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const MixedArgs a, float2 *buf, int *flags)
+{
+    extern __shared__ float2 wsm[];
+    const int n = a.g.n, tc = a.g.tc;
+    const long long N = a.g.N;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int lda = n + 1;
+    float2 *sH = wsm + (size_t)wib * (2 * n * lda + n);
+    float2 *sZ = sH + n * lda, *sTau = sZ + n * lda;
+    const SmemMat H{sH, lda}, Z{sZ, lda};
+    const long long nn = (long long)n * n;
+    const long long gw = (long long)blockIdx.x * (kWarpSchurThreads / 32) + wib;
+    const long long nw = (long long)gridDim.x * (kWarpSchurThreads / 32);
+    const int j = lane + 1;  // the row / column this lane owns
+    const float ulp = lim<float>::eps();
+    const float smlnum = lim<float>::tiny() * ((float)n / ulp);
+
+    for (long long m = gw; m < N; m += nw) {
+        // ---- load A (FP64 SoA) into H as FP32; non-finite / out-of-range check
+        const long long mo = soa_off_m(m, nn, tc);
+        bool bad = false;
+        float s2 = 0.f;
+        for (int e = lane; e < nn; e += 32) {
+            const long long k = mo + (long long)e * tc;
+            const double re = a.rA[k], im = a.iA[k];
+            bad |= nonfinite(re) | nonfinite(im);
+            const float fr = (float)re, fi = (float)im;
+            s2 = fmaf(fi, fi, fmaf(fr, fr, s2));
+            sH[(e % n) + (e / n) * lda] = make_float2(fr, fi);
+        }
+        const float nA2 = warp_sum(s2);
+        bool fb = __any_sync(FULL, bad) || !(nA2 < 1e36f);
+        int status = 0, sweeps = 0;
+        __syncwarp();
+        if (!fb) {
+            hess32_warp(n, H, sTau, lane);
+            // ---- zung2r: Z = Q from the reflectors, last reflector first
+            for (int i = n - 1; i >= 1; --i) {
+                const cx<float> t = mk(sTau[i - 1].x, sTau[i - 1].y);
+                const int c = i + 1;
+                if (j >= c + 1 && j <= n) {
+                    cx<float> sacc = Z.ld(c, j);
+                    for (int k = c + 1; k <= n; ++k) sacc = cjmac(sacc, H.ld(k, i), Z.ld(k, j));
+                    const cx<float> ts = cmul(t, sacc);
+                    Z.st(c, j, csub(Z.ld(c, j), ts));
+                    for (int k = c + 1; k <= n; ++k) Z.st(k, j, cnmac(Z.ld(k, j), H.ld(k, i), ts));
+                }
+                __syncwarp();
+                if (j >= c + 1 && j <= n) Z.st(j, c, cmul(H.ld(j, i), mk(-t.r, -t.i)));
+                if (j == c) Z.st(c, c, mk(1.f - t.r, -t.i));
+                if (j >= 2 && j <= c - 1) Z.st(j, c, mk(0.f, 0.f));
+                __syncwarp();
+            }
+            if (j <= n) {
+                Z.st(j, 1, mk(j == 1 ? 1.f : 0.f, 0.f));
+                if (j > 1) Z.st(1, j, mk(0.f, 0.f));
+            }
+            // clear below the subdiagonal: column j, rows j+2..n
+            if (j <= n)
+                for (int k = j + 2; k <= n; ++k) H.st(k, j, mk(0.f, 0.f));
+            __syncwarp();
+            // ---- make the subdiagonal real
+            for (int i = 2; i <= n; ++i) {
+                const cx<float> h = H.ld(i, i - 1);
+                if (h.i != 0.f) {
+                    cx<float> sc = cscal(h, 1.f / cabs1(h));
+                    sc = cscal(conj(sc), 1.f / cabs(sc));
+                    __syncwarp();
+                    if (lane == 0) H.st(i, i - 1, mk(cabs(h), 0.f));
+                    if (j >= i && j <= n) H.st(i, j, cmul(H.ld(i, j), sc));
+                    __syncwarp();
+                    const int re = (i + 1) < n ? (i + 1) : n;
+                    if (j <= re) H.st(j, i, cmulc(H.ld(j, i), sc));
+                    if (j <= n) Z.st(j, i, cmulc(Z.ld(j, i), sc));
+                }
+                __syncwarp();
+            }
+            // ---- single-shift QR, one matrix, uniform control flow
+            int I = n, L = 1, its = 0;
+            while (I > 1) {
+                if (its > a.max_its) { status |= ST_ITCAP; --I; L = 1; its = 0; continue; }
+                L = deflation_scan<float>(I, L, H, n, ulp, smlnum);
+                __syncwarp();
+                if (L > 1 && lane == 0) H.st(L, L - 1, mk(0.f, 0.f));
+                __syncwarp();
+                if (L >= I) { --I; L = 1; its = 0; continue; }
+                const cx<float> t = qr_shift<float>(I, L, its, H);
+                const cx<float> h11s = csub(H.ld(L, L), t);
+                const float h21 = H.ld(L + 1, L).r;
+                const float rs = 1.f / (cabs1(h11s) + fabsf(h21));
+                const cx<float> v0 = cscal(h11s, rs), v1 = mk(h21 * rs, 0.f);
+                ++its;
+                ++sweeps;
+                for (int K = L; K <= I - 1; ++K) {
+                    cx<float> a0 = v0, a1 = v1, t1;
+                    if (K > L) { a0 = H.ld(K, K - 1); a1 = H.ld(K + 1, K - 1); }
+                    zlarfg2<float>(a0, a1, t1);
+                    __syncwarp();
+                    if (K > L && lane == 0) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(0.f, 0.f)); }
+                    const cx<float> w1 = a1, cw = conj(w1), c1 = conj(t1);
+                    const float t2 = t1.r * w1.r - t1.i * w1.i;
+                    if (j >= K && j <= n) {  // rows K, K+1, column j
+                        cx<float> h1 = H.ld(K, j), h2 = H.ld(K + 1, j);
+                        rot_pair(h1, h2, c1, t2, w1);
+                        H.st(K, j, h1);
+                        H.st(K + 1, j, h2);
+                    }
+                    __syncwarp();
+                    const int je = (K + 2) < I ? (K + 2) : I;
+                    if (j <= je) {  // columns K, K+1, row j
+                        cx<float> h1 = H.ld(j, K), h2 = H.ld(j, K + 1);
+                        rot_pair(h1, h2, t1, t2, cw);
+                        H.st(j, K, h1);
+                        H.st(j, K + 1, h2);
+                    }
+                    if (j <= n) {  // Schur vectors, row j
+                        cx<float> z1 = Z.ld(j, K), z2 = Z.ld(j, K + 1);
+                        rot_pair(z1, z2, t1, t2, cw);
+                        Z.st(j, K, z1);
+                        Z.st(j, K + 1, z2);
+                    }
+                    __syncwarp();
+                }
+                // make H(I, I-1) real
+                const cx<float> h = H.ld(I, I - 1);
+                if (h.i != 0.f) {
+                    const float d = cabs(h);
+                    const cx<float> z = conj(cscal(h, 1.f / d));
+                    __syncwarp();
+                    if (lane == 0) H.st(I, I - 1, mk(d, 0.f));
+                    if (j >= I + 1 && j <= n) H.st(I, j, cmul(H.ld(I, j), z));
+                    if (j <= I - 1) H.st(j, I, cmulc(H.ld(j, I), z));
+                    if (j <= n) Z.st(j, I, cmulc(Z.ld(j, I), z));
+                }
+                __syncwarp();
+            }
+            if (status & ST_ITCAP) fb = true;
+        }
+        float2 *out = buf + m * mat_elems(n);
+        if (!fb) {
+            // T (upper triangle) and Z to the buffer, coalesced
+            for (int e = lane; e < nn; e += 32) {
+                const int r = e % n, c = e / n;
+                out[e] = r <= c ? sH[r + c * lda] : make_float2(0.f, 0.f);
+                out[nn + e] = sZ[r + c * lda];
+            }
+            __syncwarp();
+            // T-eigenvectors: lane j solves column j into sZ (Z is saved)
+            if (j <= n) {
+                const SmemCol xc{sZ + (j - 1) * lda};
+                const cx<float> tkk = H.ld(j, j);
+                const float smin = fmaxf(ulp * cabs1(tkk), smlnum);
+                const float sc = j > 1 ? trevc_solve<float>(j, H, xc, smin, tkk) : 1.f;
+                xc.st(j, mk(sc, 0.f));
+                for (int i = j + 1; i <= n; ++i) xc.st(i, mk(0.f, 0.f));
+            }
+            __syncwarp();
+            for (int e = lane; e < nn; e += 32) out[2 * nn + e] = sZ[(e % n) + (e / n) * lda];
+        }
+        if (lane == 0) {
+            out[3 * nn] = make_float2(nA2, 0.f);  // ||A||_F^2 for the refinement's tolerance
+            flags[m] = fb ? 1 : 0;
+            if (fb) to_fp64_list(a, flags, m);
+            if (a.status) a.status[m] = status;
+            if (a.sweeps) a.sweeps[m] = sweeps;
+        }
+        __syncwarp();
+    }
+}
+
+// FP32 matrix in the Schur buffer, element stride S: 32 in the group layout
+// of schur32_kernel, 1 in the per-matrix layout of schur32_warp_kernel.
+template <int S> struct MatBuf {
+    float2 *p;
+    int n;
+    __device__ __forceinline__ cx<float> ld(int i, int j) const
+    {
+        const float2 v = p[((i - 1) + (j - 1) * n) * S];
+        return mk(v.x, v.y);
+    }
+};
+
 // One eigenpair per lane.  MAXN bounds n (per-lane vectors live in local
-// memory, indexed uniformly across the warp).
-template <int MAXN>
+// memory, indexed uniformly across the warp).  kPerMatrix: the Schur buffer
+// has the per-matrix layout.
+template <int MAXN, bool kPerMatrix>
 __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs a, const float2 *buf, int *flags)
 {
     const int n = a.g.n, tc = a.g.tc;
@@ -146,9 +353,11 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
     if (!__any_sync(FULL, act)) return;
 
     const long long nn = (long long)n * n;
-    float2 *pT = const_cast<float2 *>(buf) + (m / 32) * group_elems(n) * 32 + (m % 32);
-    const MatIlv<float> T{pT, n}, Z{pT + 32 * nn, n}, X{pT + 64 * nn, n};
-    const float nA2 = pT[96 * nn].x;
+    constexpr int S = kPerMatrix ? 1 : 32;
+    float2 *pT = const_cast<float2 *>(buf) +
+                 (kPerMatrix ? m * mat_elems(n) : (m / 32) * group_elems(n) * 32 + (m % 32));
+    const MatBuf<S> T{pT, n}, Z{pT + S * nn, n}, X{pT + 2 * S * nn, n};
+    const float nA2 = pT[3 * S * nn].x;
     const long long mo = soa_off_m(m, nn, tc);
     const MatSoA<double> A{const_cast<double *>(a.rA) + mo, const_cast<double *>(a.iA) + mo, tc, n};
 
@@ -265,6 +474,48 @@ size_t mixed_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blo
     return bufb + flagb;
 }
 
+namespace {
+
+// Which FP32 Schur kernel: the warp-per-matrix one for 24 <= n <= 32 (measured
+// on GB300, FP32+refine eigensolves/s lane -> warp: n=16 5.34 -> 4.26 M/s,
+// n=24 1.59 -> 1.63 M/s, n=32 0.66 -> 0.72 M/s: below 24 too many lanes idle
+// and the serial reflector steps dominate), the lane-per-matrix one otherwise.  VES_MIXED_SCHUR=lane|warp overrides (for tests and tuning;
+// warp only applies to n <= 32).
+bool use_warp_schur(int n)
+{
+    int mode = 0;  // 0 auto, 1 lane, 2 warp; read per launch (a getenv is cheap next to a solve)
+    if (const char *e = getenv("VES_MIXED_SCHUR")) {
+        if (!strcmp(e, "lane")) mode = 1;
+        if (!strcmp(e, "warp")) mode = 2;
+    }
+    if (n > 32 || mode == 1) return false;
+    return mode == 2 || n >= 24;
+}
+
+long long warp_schur_blocks(int n, long long N, int blocks_per_sm)
+{
+    static int attr_set = 0, sms = 0;
+    if (!attr_set) {
+        cudaFuncSetAttribute(schur32_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)warp_schur_smem(32));
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        attr_set = 1;
+    }
+    int per_sm = blocks_per_sm;
+    if (per_sm <= 0) {
+        per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, schur32_warp_kernel, kWarpSchurThreads,
+                                                      warp_schur_smem(n));
+        if (per_sm < 1) per_sm = 1;
+    }
+    const long long need = (N + kWarpSchurThreads / 32 - 1) / (kWarpSchurThreads / 32);
+    return std::max<long long>(1, std::min<long long>(need, (long long)std::max(sms, 1) * per_sm));
+}
+
+}  // namespace
+
 cudaError_t launch_mixed(const MixedArgs &a, cudaStream_t st)
 {
     if (a.g.N <= 0) return cudaSuccess;
@@ -274,17 +525,28 @@ cudaError_t launch_mixed(const MixedArgs &a, cudaStream_t st)
     float2 *buf = static_cast<float2 *>(a.ws);
     int *flags = reinterpret_cast<int *>(static_cast<char *>(a.ws) +
                                          (size_t)groups * group_elems(n) * 32 * sizeof(float2));
-    schur32_kernel<<<(unsigned)schur_blocks(a.g.N, a.blocks_per_sm), kSchurThreads, 0, st>>>(a, buf, flags);
+    const bool warp = use_warp_schur(n);
+    if (warp)
+        schur32_warp_kernel<<<(unsigned)warp_schur_blocks(n, a.g.N, a.blocks_per_sm), kWarpSchurThreads,
+                              warp_schur_smem(n), st>>>(a, buf, flags);
+    else
+        schur32_kernel<<<(unsigned)schur_blocks(a.g.N, a.blocks_per_sm), kSchurThreads, 0, st>>>(a, buf, flags);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const long long pairs = a.g.N * n;
     const unsigned rb = (unsigned)((pairs + kRefineThreads - 1) / kRefineThreads);
-    if (n <= 16)
-        refine_kernel<16><<<rb, kRefineThreads, 0, st>>>(a, buf, flags);
-    else if (n <= 32)
-        refine_kernel<32><<<rb, kRefineThreads, 0, st>>>(a, buf, flags);
-    else
-        refine_kernel<64><<<rb, kRefineThreads, 0, st>>>(a, buf, flags);
+    if (warp) {
+        if (n <= 16)
+            refine_kernel<16, true><<<rb, kRefineThreads, 0, st>>>(a, buf, flags);
+        else
+            refine_kernel<32, true><<<rb, kRefineThreads, 0, st>>>(a, buf, flags);
+    } else if (n <= 16) {
+        refine_kernel<16, false><<<rb, kRefineThreads, 0, st>>>(a, buf, flags);
+    } else if (n <= 32) {
+        refine_kernel<32, false><<<rb, kRefineThreads, 0, st>>>(a, buf, flags);
+    } else {
+        refine_kernel<64, false><<<rb, kRefineThreads, 0, st>>>(a, buf, flags);
+    }
     return cudaGetLastError();
 }
 

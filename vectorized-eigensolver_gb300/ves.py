@@ -81,6 +81,7 @@ SIGNATURES = {
     "ves_graph_capture_varsize": (_int, [ctypes.POINTER(_VP), ctypes.c_longlong, _int, _VP, _VP, _VP, _VP, _VP, _VP,
                                          _VP, _VP, _VP, ctypes.POINTER(Options), _VP, _size]),
     "ves_graph_launch": (_int, [_VP, _VP]),
+    "ves_eigensolve_shifts_workspace_size": (_size, [_int, _int, _int, ctypes.POINTER(Options)]),
     "ves_eigensolve_shifts": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
                                      ctypes.POINTER(Options), _VP, _size, _VP]),
     "ves_shiftnet_create": (_int, [ctypes.POINTER(_VP), _int, _int, _int, ctypes.c_ulonglong]),
@@ -386,6 +387,12 @@ def eigensolve_shifts(dim, block_cnt, thread_cnt, rA, iA, rE, iE, rV, iV, rS, iS
     _check(lib().ves_eigensolve_shifts(dim, block_cnt, thread_cnt, _dp(rA), _dp(iA), _dp(rE), _dp(iE), _dp(rV),
                                        _dp(iV), _dp(rS), _dp(iS), _dp(status), _dp(sweeps), _dp(fallbacks),
                                        ctypes.byref(o), ws_ptr, ws_n, _stream_ptr(stream)), "ves_eigensolve_shifts")
+
+
+def shifts_workspace(dim, block_cnt, thread_cnt, options=None):
+    """A device workspace for ves_eigensolve_shifts with these options."""
+    o = options if options is not None else default_options()
+    return DeviceBuffer(lib().ves_eigensolve_shifts_workspace_size(dim, block_cnt, thread_cnt, ctypes.byref(o)))
 
 
 class ShiftNet:
