@@ -22,6 +22,18 @@ roofline  the solver is FP64-pipe bound: achieved = algorithmic FP64 flops
         beside it.
 cpu_baseline  the oracle's C restatement of the reference CPU path (OpenMP,
         all host cores) on a bounded prefix of the same batch.
+forms   the other forms, each on its own batch, each verified (residuals on the
+        device; learned: eigenvalues against the plain solve):
+        FP32+refine  n=16 (the same batch) and n=32 (262,144 Gaussian, seed 3,
+                     beside plain FP64 on the same batch);
+        learned shift  n=16 and n=32 on the family A0 + p1 A1 + p2 A2 + p3 A3
+                     (262,144 matrices, parameter seed 6): the network is
+                     trained first (200,000 plain-solver solutions, seed 5; not
+                     timed), then one step = inference + polish + shift-seeded
+                     FP64 solve, against plain FP64 on the same batch;
+        mixed-size   500,000 matrices of orders 4..64 (Gaussian, non-normal,
+                     clustered; seed 2): one CUDA-graph replay of the binned
+                     persistent solve against one launch per order.
 Every result is verified after timing: all residuals on the device in FP64
 (<= 1e-13 of ||A||_F ||v||); eigenvalue parity with the oracle is the job of
 the test suite (tests/test_gpu_fullsize.py runs this workload).
@@ -59,6 +71,14 @@ def log(*a):
 # ----------------------------------------------------------------------------
 # distributed plumbing (one process per GPU; independent replicas, no data-path collective)
 # ----------------------------------------------------------------------------
+def rank_batch(rank):
+    """The batch rank `rank` solves: the benchmark workload with seed 1 + rank
+    (weak scaling: every GPU gets its own 1,048,576 matrices; no data-path
+    exchange between ranks)."""
+    w = WORKLOAD
+    return dict(N=w["N"], n=w["n"], tc=w["tc"], seed=w["seed"] + rank)
+
+
 class Dist:
     def __init__(self):
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -171,8 +191,8 @@ def run_reference_arm(args, d):
     import workloads
     cores = os.cpu_count() or 1
     kind, lib = cpu_kind()
-    sample = 65_536
-    rA, iA = workloads.gaussian_soa(w["N"], w["n"], w["seed"], w["tc"])
+    sample = args.ref_sample
+    rA, iA = workloads.gaussian_soa(w["N"], w["n"], w["seed"], w["tc"])  # the batch; its first `sample` matrices
     k = sample * w["n"] ** 2
     rA, iA = rA[:k].copy(), iA[:k].copy()
     for _ in range(max(args.warmup, 0)):
@@ -289,13 +309,19 @@ def eig_distance(E1, E0, A, chunk=1 << 17):
     return worst
 
 
-LEARNED_NET = dict(hidden=256, layers=4, fourier=8, loss=1, delta=0.01)  # ves_shiftnet_config
-LEARNED_EPOCHS = 150
-LEARNED_POLISH = 6     # Newton steps per prediction (FP32, on the Hessenberg form)
-LEARNED_GATE = 3e-2    # predictions only while |H(I,I-1)| > gate * ||A||_F / sqrt(n)
+# Learned-shift configuration per order (chosen on GB300 by sweeping depth,
+# Fourier features, epochs, polish steps and gate on a held-out draw):
+#   net     ves_shiftnet_config fields (robust Chamfer loss, delta 0.01)
+#   epochs  over the 200,000 training solutions
+#   polish  Newton steps per prediction (FP32, on the Hessenberg form)
+#   gate    predictions only while |H(I,I-1)| > gate * ||A||_F / sqrt(n)
+LEARNED = {
+    16: dict(net=dict(hidden=256, layers=4, fourier=8, loss=1, delta=0.01), epochs=150, polish=6, gate=3e-2),
+    32: dict(net=dict(hidden=256, layers=5, fourier=12, loss=1, delta=0.01), epochs=300, polish=10, gate=3e-2),
+}
 
 
-def measure_learned(n, N, train_count, epochs, steps, tc=512):
+def measure_learned(n, N, train_count, steps, tc=512):
     """The learned-shift form on the parametric family A(p) = A0 + p1 A1 + p2 A2
     + p3 A3 (order n): the network is trained (tcgen05 BF16 MLP) on
     `train_count` plain-solver solutions (param seed 5), then on a fresh batch
@@ -305,8 +331,10 @@ def measure_learned(n, N, train_count, epochs, steps, tc=512):
     import torch
     import ves
     import learned_shift
+    cfg = LEARNED[n]
+    epochs = cfg["epochs"]
     t0 = time.perf_counter()
-    net, losses = learned_shift.train(n, count=train_count, epochs=epochs, batch=1024, lr=1e-3, **LEARNED_NET)
+    net, losses = learned_shift.train(n, count=train_count, epochs=epochs, batch=1024, lr=1e-3, **cfg["net"])
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     p, rA, iA = learned_shift.family(N, n, param_seed=6, thread_cnt=tc)
@@ -317,7 +345,7 @@ def measure_learned(n, N, train_count, epochs, steps, tc=512):
     rV, iV = torch.empty_like(rA), torch.empty_like(iA)
     sw0, sw, st, fb = (torch.zeros(N, dtype=torch.int32, device="cuda") for _ in range(4))
     ws = ves.Workspace(n, bc, tc)
-    lopt = ves.default_options(shift_polish=LEARNED_POLISH, shift_gate=LEARNED_GATE)
+    lopt = ves.default_options(shift_polish=cfg["polish"], shift_gate=cfg["gate"])
     lws = ves.shifts_workspace(n, bc, tc, lopt)
     pws = net.predict_workspace(N)
     stream = torch.cuda.current_stream()
@@ -361,8 +389,8 @@ def measure_learned(n, N, train_count, epochs, steps, tc=512):
            "fallback_per_eigenvalue": float(fb.double().mean()) / n,
            "prediction_error_median_rel": float((pred_err / nA[:, None]).median()),
            "train": {"matrices": train_count, "epochs": epochs, "seconds": train_s, "loss_first": losses[0],
-                     "loss_last": losses[-1], "network": LEARNED_NET},
-           "shift_polish": LEARNED_POLISH, "shift_gate": LEARNED_GATE,
+                     "loss_last": losses[-1], "network": cfg["net"]},
+           "shift_polish": cfg["polish"], "shift_gate": cfg["gate"],
            "max_residual": ver["max_residual"], "nonfinite": ver["nonfinite"], "max_eig_err_rel": err,
            "passed": ver["max_residual"] <= RES_TOL and ver["nonfinite"] == 0 and err <= 1e-12 and other == 0}
     del net, rA, iA, rV, iV, ws, lws, pws, A
@@ -468,7 +496,7 @@ def run_gpu_arm(args, d):
     w = WORKLOAD
     N, n, tc = w["N"], w["n"], w["tc"]
     bc = N // tc
-    seed = w["seed"] + d.rank  # each rank solves its own batch (weak scaling)
+    seed = rank_batch(d.rank)["seed"]  # each rank solves its own batch (weak scaling)
     log("[bench] generating %d x %dx%d seed %d" % (N, n, n, seed))
     rA, iA = workloads.gaussian_soa(N, n, seed, tc)
     dAr = torch.from_numpy(rA).cuda()
@@ -553,7 +581,7 @@ def run_gpu_arm(args, d):
         forms += [p32, m32]
         for ln in (16, 32):
             log("[bench] learned-shift form, n=%d" % ln)
-            forms.append(measure_learned(ln, 262_144, 200_000, LEARNED_EPOCHS, 2))
+            forms.append(measure_learned(ln, 262_144, 200_000, 2))
         log("[bench] mixed-size form")
         forms.append(measure_varsize(500_000, 2))
 
@@ -682,6 +710,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ves", choices=["ves", "reference"])
+    ap.add_argument("--ref-sample", type=int, default=65_536,
+                    help="matrices per step of the CPU reference arm (a prefix of the batch)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
