@@ -170,7 +170,7 @@ def cpu_time(rA, iA, n, tc, threads, lib, min_seconds):
     N = rA.size // (n * n)
     reps, total = 0, 0.0
     oracle.eigensolve(rA, iA, n, tc, lib=lib, threads=threads)  # warm-up
-    while total < min_seconds:
+    while reps == 0 or total < min_seconds:
         t0 = time.perf_counter()
         oracle.eigensolve(rA, iA, n, tc, lib=lib, threads=threads)
         total += time.perf_counter() - t0
@@ -665,7 +665,9 @@ def run_ncu_case(args):
     --ncu-form solve:    FP64 then FP32+refine on N Gaussian n x n matrices;
     --ncu-form shiftnet: network inference (4 tcgen05 GEMMs) on N family matrices
                          (untrained weights: the kernels do the same work);
-    --ncu-form varsize:  one mixed-size solve of N family matrices (orders 4..64)."""
+    --ncu-form varsize:  one mixed-size solve of N family matrices (orders 4..64);
+    --ncu-form learned:  polish pre-pass + shift-seeded FP64 solve of N family
+                         matrices (predictions: eigenvalues + 1% noise)."""
     import torch
     import ves
     n, N, tc = args.ncu_n, args.ncu_case, 512
@@ -678,6 +680,20 @@ def run_ncu_case(args):
         net.predict(N, tc, p, rA, iA, rS, iS)
         torch.cuda.synchronize()
         print("ncu case done: shift network inference on %d matrices, n=%d" % (N, n))
+        return
+    if args.ncu_form == "learned":
+        import learned_shift
+        p, rA, iA = learned_shift.family(N, n, param_seed=6, thread_cnt=tc)
+        rE0, iE0, _ = learned_shift.solve_plain(n, N, rA, iA, tc)
+        g = torch.Generator(device="cuda").manual_seed(1)
+        rS = rE0 + 1e-2 * torch.randn(rE0.shape, generator=g, device="cuda", dtype=torch.float64)
+        iS = iE0 + 1e-2 * torch.randn(rE0.shape, generator=g, device="cuda", dtype=torch.float64)
+        rE, iE = torch.empty_like(rE0), torch.empty_like(iE0)
+        rV, iV = torch.empty_like(rA), torch.empty_like(iA)
+        ves.eigensolve_shifts(n, N // tc, tc, rA, iA, rE, iE, rV, iV, rS, iS,
+                              options=ves.default_options(shift_polish=6, shift_gate=3e-2))
+        torch.cuda.synchronize()
+        print("ncu case done: polish pre-pass + shift-seeded solve of %d family matrices, n=%d" % (N, n))
         return
     if args.ncu_form == "varsize":
         import workloads
@@ -719,7 +735,7 @@ def main():
     ap.add_argument("--ncu-case", type=int, default=0, metavar="N",
                     help="no benchmark: one solve per form on N matrices (for ncu captures)")
     ap.add_argument("--ncu-n", type=int, default=16)
-    ap.add_argument("--ncu-form", default="solve", choices=["solve", "shiftnet", "varsize"])
+    ap.add_argument("--ncu-form", default="solve", choices=["solve", "shiftnet", "varsize", "learned"])
     args = ap.parse_args()
     if args.ncu_case:
         run_ncu_case(args)

@@ -64,7 +64,7 @@ def test_reference_arm_two_ranks():
     pytest.importorskip("torch")
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
            "127.0.0.1", "--master-port", str(free_port()), os.path.join(ROOT, "bench.py"), "--impl", "reference",
-           "--gpus", "2", "--steps", "1", "--warmup", "0", "--ref-sample", "512"]
+           "--gpus", "2", "--steps", "2", "--warmup", "1", "--ref-sample", "512"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
