@@ -114,19 +114,6 @@ cudaError_t launch_varsize(long long count, int max_dim, const int *dims, const 
 cudaError_t launch_gemm_bf16(int M, int N, int K, const void *A, int lda, const void *Bt, int ldb, const float *bias,
                              int act, void *C, float *Cf, int ldc, int *err, cudaStream_t st);
 
-// Ask for the largest L1 / smallest shared-memory split for a kernel that uses
-// no shared memory (the FP64 workspace kernels stream per-warp matrices through
-// L1); once per kernel, unless VES_L1_CARVEOUT=default.
-template <class K> inline void prefer_l1(K kernel, bool &done)
-{
-    if (done) return;
-    done = true;
-    const char *e = getenv("VES_L1_CARVEOUT");
-    if (e && e[0] == 'd') return;
-    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
-    cudaGetLastError();
-}
-
 // Record the calling thread's message for ves_last_error().
 void set_error_message(const char *msg);
 

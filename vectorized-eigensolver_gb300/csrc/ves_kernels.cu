@@ -451,14 +451,10 @@ cudaError_t launch_fused_fp64(const FusedArgs &a, cudaStream_t st)
     if (a.g.N <= 0) return cudaSuccess;
     int blocks = 0, threads = 0;
     fused_workspace_bytes(a.g.n, a.g.N, a.blocks_per_sm, &blocks, &threads, a.rS != nullptr);
-    static bool l1_learned = false, l1_plain = false;
-    if (a.rS) {
-        prefer_l1(fused_fp64_kernel<true>, l1_learned);
+    if (a.rS)
         fused_fp64_kernel<true><<<blocks, threads, 0, st>>>(a);
-    } else {
-        prefer_l1(fused_fp64_kernel<false>, l1_plain);
+    else
         fused_fp64_kernel<false><<<blocks, threads, 0, st>>>(a);
-    }
     return cudaGetLastError();
 }
 

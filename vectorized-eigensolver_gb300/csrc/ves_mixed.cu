@@ -526,14 +526,11 @@ cudaError_t launch_mixed(const MixedArgs &a, cudaStream_t st)
     int *flags = reinterpret_cast<int *>(static_cast<char *>(a.ws) +
                                          (size_t)groups * group_elems(n) * 32 * sizeof(float2));
     const bool warp = use_warp_schur(n);
-    static bool l1 = false;
-    if (warp) {
+    if (warp)
         schur32_warp_kernel<<<(unsigned)warp_schur_blocks(n, a.g.N, a.blocks_per_sm), kWarpSchurThreads,
                               warp_schur_smem(n), st>>>(a, buf, flags);
-    } else {
-        prefer_l1(schur32_kernel, l1);
+    else
         schur32_kernel<<<(unsigned)schur_blocks(a.g.N, a.blocks_per_sm), kSchurThreads, 0, st>>>(a, buf, flags);
-    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const long long pairs = a.g.N * n;

@@ -295,8 +295,6 @@ cudaError_t launch_varsize(long long count, int max_dim, const int *dims, const 
     a.status = status; a.sweeps = sweeps;
     a.aoff = aoff; a.eoff = eoff; a.sorted = sorted; a.items = items; a.nitems = nitems; a.next_item = next;
     a.ws = w + p.slots; a.max_dim = max_dim; a.max_its = max_its; a.vnorm = vnorm;
-    static bool l1 = false;
-    prefer_l1(varsize_solve_kernel, l1);
     varsize_solve_kernel<<<(unsigned)(p.nslots / (kSolveThreads / 32)), kSolveThreads, 0, st>>>(a);
     return cudaGetLastError();
 }
