@@ -1,8 +1,12 @@
 """Full-size workloads: every matrix checked on the device in FP64, the
 oracle on a prefix.
 
+     10,000 x 8x8,   seed 0  (all against the oracle)
   1,048,576 x 16x16, seed 1  (oracle on the first 65,536)
     262,144 x 32x32, seed 3  (oracle on the first 16,384)
+    500,000 mixed orders 4..64, seed 2, three families (oracle on the first 3,000)
+  1,048,576 x 24x24 learned-shift family (oracle on the first 4,096)
+The FP32 + refinement form at 262,144 x 32x32 is in test_gpu_mixed.py.
 """
 import numpy as np
 import pytest
@@ -53,3 +57,121 @@ def test_fullsize_plain_fp64(name):
     assert (err / np.linalg.norm(Ah, axis=(1, 2))).max() <= 1e-12
     assert same.mean() > 0.99
     assert (sw[:sub].cpu().numpy() == swo).mean() > 0.99
+
+
+def test_fullsize_gauss8_all_vs_oracle():
+    """10,000 x 8x8, seed 0 (the reference's CPU configuration), thread_cnt 4:
+    every matrix against the oracle."""
+    import torch
+    w = workloads.WORKLOADS["gauss8"]
+    N, n, seed, tc = w["N"], w["n"], w["seed"], 4
+    rA, iA = workloads.gaussian_soa(N, n, seed, tc)
+    dA = [torch.from_numpy(x).cuda() for x in (rA, iA)]
+    dE = [torch.empty(N * n, dtype=torch.float64, device="cuda") for _ in range(2)]
+    dV = [torch.empty_like(dA[0]) for _ in range(2)]
+    st = torch.full((N,), -1, dtype=torch.int32, device="cuda")
+    ves.eigensolve(n, N // tc, tc, dA[0], dA[1], dE[0], dE[1], dV[0], dV[1], status=st)
+    torch.cuda.synchronize()
+    assert int((st != 0).sum()) == 0
+    res = device_residuals(soa_planes_to_batch(dA[0], dA[1], n, tc), soa_vec_to_batch(dE[0], dE[1], n, tc),
+                           soa_planes_to_batch(dV[0], dV[1], n, tc))
+    assert float(res.max()) <= 1e-13
+    rE, iE, *_ = oracle.eigensolve(rA, iA, n, tc)
+    Eo = ves.complex_vec_from_soa(rE, iE, n, tc)
+    Eg = ves.complex_vec_from_soa(dE[0].cpu().numpy(), dE[1].cpu().numpy(), n, tc)
+    A = ves.complex_from_soa(rA, iA, n, tc)
+    _, err, _ = match_eigs(Eg, Eo)
+    assert (err / np.linalg.norm(A, axis=(1, 2))).max() <= 1e-12
+
+
+def test_fullsize_varsize_families():
+    """500,000 matrices of orders 4..64 (Gaussian / non-normal / clustered,
+    seed 2) in one mixed-size solve: every residual on the device; the first
+    3,000 matrices against the oracle.  Eigenvalue agreement is held to
+    1e-12 ||A||_F except for the non-normal family, whose eigenvalues have
+    condition numbers up to cond(V) = 1e4: two backward-stable solvers may then
+    differ by up to cond(V) times that bar."""
+    import torch
+    N = 500_000
+    sizes, by_n = workloads.mixed_families(N, seed=2, device="cuda", as_list=False)
+    dims, re, im = workloads.pack_varsize(sizes, by_n, device="cuda")
+    er = torch.empty(int(sizes.sum()), dtype=torch.float64, device="cuda")
+    ei, vr, vi = torch.empty_like(er), torch.empty_like(re), torch.empty_like(im)
+    st = torch.full((N,), -1, dtype=torch.int32, device="cuda")
+    ves.eigensolve_varsize(N, 64, dims, re, im, er, ei, vr, vi, status=st)
+    torch.cuda.synchronize()
+    assert int((st != 0).sum()) == 0
+    off = np.concatenate([[0], np.cumsum(sizes.astype(np.int64) ** 2)])
+    eoff = np.concatenate([[0], np.cumsum(sizes.astype(np.int64))])
+    for n, (idx, _) in by_n.items():
+        o2 = torch.from_numpy(off[idx]).cuda()[:, None] + torch.arange(n * n, device="cuda")[None]
+        e2 = torch.from_numpy(eoff[idx]).cuda()[:, None] + torch.arange(n, device="cuda")[None]
+        A = torch.complex(re[o2], im[o2]).view(-1, n, n).transpose(1, 2)
+        V = torch.complex(vr[o2], vi[o2]).view(-1, n, n).transpose(1, 2)
+        E = torch.complex(er[e2], ei[e2])
+        r = torch.linalg.vector_norm(A @ V - V * E[:, None, :], dim=1)
+        q = r / (torch.linalg.matrix_norm(A)[:, None] * torch.linalg.vector_norm(V, dim=1))
+        assert float(q.max()) <= 1e-13, (n, float(q.max()))
+    # oracle on the first 3,000 matrices, one SoA batch per order
+    sub = 3000
+    fam = np.arange(sub) % 3
+    worst = {0: 0.0, 1: 0.0, 2: 0.0}
+    rh, ih = re.cpu().numpy(), im.cpu().numpy()
+    erh, eih = er.cpu().numpy(), ei.cpu().numpy()
+    for n in np.unique(sizes[:sub]):
+        ids = np.nonzero(sizes[:sub] == n)[0]
+        A = np.stack([(rh[off[m]:off[m + 1]] + 1j * ih[off[m]:off[m + 1]]).reshape(n, n).T for m in ids])
+        Eg = np.stack([erh[eoff[m]:eoff[m + 1]] + 1j * eih[eoff[m]:eoff[m + 1]] for m in ids])
+        ra, ia = ves.soa_from_complex(A, 1)
+        rE, iE, *_ = oracle.eigensolve(ra, ia, int(n), 1)
+        Eo = ves.complex_vec_from_soa(rE, iE, int(n), 1)
+        _, err, _ = match_eigs(Eg, Eo)
+        rel = (err / np.linalg.norm(A, axis=(1, 2))[:, None]).max(axis=1)
+        for f in (0, 1, 2):
+            if (fam[ids] == f).any():
+                worst[f] = max(worst[f], float(rel[fam[ids] == f].max()))
+    assert worst[0] <= 1e-12 and worst[2] <= 1e-12, worst
+    assert worst[1] <= 1e-12 * 1e4, worst
+
+
+def test_fullsize_learned_config():
+    """The learned-shift configuration: 1,048,576 family matrices of order 24
+    (A0 + p1 A1 + p2 A2 + p3 A3, basis seed 4, parameter seed 6), a network
+    trained on 200,000 plain-solver solutions (parameter seed 5): every
+    residual on the device, eigenvalues against the plain solve on every
+    matrix, and against the oracle on the first 4,096."""
+    import torch
+    import learned_shift
+    n, N = 24, 1 << 20
+    net, _ = learned_shift.train(n, count=200_000, epochs=40, layers=4, fourier=8, loss=1, delta=0.01)
+    p, rA, iA = learned_shift.family(N, n, param_seed=6, thread_cnt=TC)
+    rE0, iE0, sw0 = learned_shift.solve_plain(n, N, rA, iA, TC)
+    rS, iS = learned_shift.predict(net, n, N, p, rA, iA, TC)
+    rE, iE = torch.empty_like(rE0), torch.empty_like(iE0)
+    rV, iV = torch.empty_like(rA), torch.empty_like(iA)
+    st = torch.full((N,), -1, dtype=torch.int32, device="cuda")
+    sw = torch.zeros(N, dtype=torch.int32, device="cuda")
+    ves.eigensolve_shifts(n, N // TC, TC, rA, iA, rE, iE, rV, iV, rS, iS, status=st, sweeps=sw,
+                          options=ves.default_options(shift_polish=6, shift_gate=3e-2))
+    torch.cuda.synchronize()
+    assert int(((st & ~ves.VES_STATUS_SHIFT_FALLBACK) != 0).sum()) == 0
+    A = soa_planes_to_batch(rA, iA, n, TC)
+    E = soa_vec_to_batch(rE, iE, n, TC)
+    res = device_residuals(A, E, soa_planes_to_batch(rV, iV, n, TC))
+    assert float(res.max()) <= 1e-13
+    E0 = soa_vec_to_batch(rE0, iE0, n, TC)
+    nA = torch.linalg.matrix_norm(A)
+    worst = 0.0
+    for s in range(0, N, 1 << 17):
+        d = (E[s:s + (1 << 17), :, None] - E0[s:s + (1 << 17), None, :]).abs().amin(dim=2)
+        worst = max(worst, float((d / nA[s:s + (1 << 17), None]).max()))
+    assert worst <= 1e-12
+    assert float(sw.double().mean()) < float(sw0.double().mean())
+    sub = 4096
+    k = sub * n * n
+    ro, io, *_ = oracle.eigensolve(rA[:k].cpu().numpy(), iA[:k].cpu().numpy(), n, TC)
+    Eo = ves.complex_vec_from_soa(ro, io, n, TC)
+    Eg = ves.complex_vec_from_soa(rE[:sub * n].cpu().numpy(), iE[:sub * n].cpu().numpy(), n, TC)
+    Ah = ves.complex_from_soa(rA[:k].cpu().numpy(), iA[:k].cpu().numpy(), n, TC)
+    _, err, _ = match_eigs(Eg, Eo)
+    assert (err / np.linalg.norm(Ah, axis=(1, 2))).max() <= 1e-12
