@@ -169,7 +169,7 @@ __global__ void soa_to_aos_kernel(const double *re, const double *im, double2 *Z
     }
 }
 
-int g_extras_blocks_per_sm = 2;
+constexpr int kExtrasBlocksPerSm = 2;  // default: 8 warps per SM, as the fused kernel
 
 long long persistent_blocks(long long N, int blocks_per_sm)
 {
@@ -178,7 +178,8 @@ long long persistent_blocks(long long N, int blocks_per_sm)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
     const long long groups = (N + 31) / 32;
-    return std::max<long long>(1, std::min<long long>((groups + 3) / 4, (long long)sms * (blocks_per_sm > 0 ? blocks_per_sm : g_extras_blocks_per_sm)));
+    const int bps = blocks_per_sm > 0 ? blocks_per_sm : kExtrasBlocksPerSm;
+    return std::max<long long>(1, std::min<long long>((groups + 3) / 4, (long long)sms * bps));
 }
 
 }  // namespace

@@ -417,27 +417,32 @@ __global__ void fp64_fma_probe_kernel(double *out, int iters, double b, double c
 constexpr int kStageThreads = 128;
 inline unsigned stage_blocks(const Geom &g) { return (unsigned)((g.N + kStageThreads - 1) / kStageThreads); }
 
-int g_fused_blocks_per_sm = 2;  // 8 warps per SM; tunable through VES_FUSED_BLOCKS_PER_SM
+// default blocks (4 warps each) per SM: 8 warps; VES_FUSED_BLOCKS_PER_SM overrides
+int fused_default_bps()
+{
+    if (const char *e = getenv("VES_FUSED_BLOCKS_PER_SM")) {
+        const int v = atoi(e);
+        if (v >= 1 && v <= 16) return v;
+    }
+    return 2;
+}
+
+int device_sms()
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
 
 }  // namespace
 
 size_t fused_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blocks, int *out_threads, bool learned)
 {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-    static bool env_read = false;
-    if (!env_read) {
-        env_read = true;
-        if (const char *e = getenv("VES_FUSED_BLOCKS_PER_SM")) {
-            int v = atoi(e);
-            if (v >= 1 && v <= 16) g_fused_blocks_per_sm = v;
-        }
-    }
+    const int sms = device_sms();
     const long long groups = (N + 31) / 32;
     const int wpb = kFusedThreads / 32;
-    const int bps = blocks_per_sm > 0 ? blocks_per_sm : g_fused_blocks_per_sm;
+    const int bps = blocks_per_sm > 0 ? blocks_per_sm : fused_default_bps();
     long long blocks = std::min<long long>((groups + wpb - 1) / wpb, (long long)sms * bps);
     if (blocks < 1) blocks = 1;
     const size_t per_slot = (size_t)fused_slot_elems(n, learned) * 32 * sizeof(double2);
@@ -463,22 +468,16 @@ cudaError_t launch_polish32(Geom g, const double *rA, const double *iA, const do
 {
     if (g.N <= 0) return cudaSuccess;
     if (g.n > 32) return cudaErrorInvalidValue;
-    static bool attr = false;
-    static int sms = 0;
-    if (!attr) {
-        cudaFuncSetAttribute(polish32_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)polish_smem_bytes(32));
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        attr = true;
-    }
+    // per call (per device, thread safe; microseconds next to the kernel)
+    cudaError_t e = cudaFuncSetAttribute(polish32_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)polish_smem_bytes(32));
+    if (e != cudaSuccess) return e;
+    const int sms = device_sms();
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, polish32_warp_kernel, kPolishThreads,
                                                   polish_smem_bytes(g.n));
     const long long need = (g.N + kPolishThreads / 32 - 1) / (kPolishThreads / 32);
-    const long long blocks = std::max<long long>(1, std::min<long long>(need, (long long)std::max(sms, 1) *
-                                                                                   std::max(per_sm, 1)));
+    const long long blocks = std::max<long long>(1, std::min<long long>(need, (long long)sms * std::max(per_sm, 1)));
     polish32_warp_kernel<<<(unsigned)blocks, kPolishThreads, polish_smem_bytes(g.n), st>>>(g, rA, iA, rS, iS, rP,
                                                                                          iP, steps);
     return cudaGetLastError();

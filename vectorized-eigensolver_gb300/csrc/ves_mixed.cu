@@ -441,24 +441,29 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
     for (int i = 1; i <= n; ++i) Vo.st(i, k, cscal(v[i - 1], scale));
 }
 
-int g_schur_blocks_per_sm = 8;
+// default blocks (4 warps each) per SM of the lane Schur kernel; VES_MIXED_BLOCKS_PER_SM overrides
+int schur_default_bps()
+{
+    if (const char *e = getenv("VES_MIXED_BLOCKS_PER_SM")) {
+        const int v = atoi(e);
+        if (v >= 1 && v <= 16) return v;
+    }
+    return 8;
+}
 
-long long schur_blocks(long long N, int blocks_per_sm)
+int device_sms()
 {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-    static bool env_read = false;
-    if (!env_read) {
-        env_read = true;
-        if (const char *e = getenv("VES_MIXED_BLOCKS_PER_SM")) {
-            int v = atoi(e);
-            if (v >= 1 && v <= 16) g_schur_blocks_per_sm = v;
-        }
-    }
+    return sms > 0 ? sms : 1;
+}
+
+long long schur_blocks(long long N, int blocks_per_sm)
+{
+    const int sms = device_sms();
     const long long groups = (N + 31) / 32;
-    const int bps = blocks_per_sm > 0 ? blocks_per_sm : g_schur_blocks_per_sm;
+    const int bps = blocks_per_sm > 0 ? blocks_per_sm : schur_default_bps();
     return std::max<long long>(1, std::min<long long>((groups + 3) / 4, (long long)sms * bps));
 }
 
@@ -494,15 +499,9 @@ bool use_warp_schur(int n)
 
 long long warp_schur_blocks(int n, long long N, int blocks_per_sm)
 {
-    static int attr_set = 0, sms = 0;
-    if (!attr_set) {
-        cudaFuncSetAttribute(schur32_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)warp_schur_smem(32));
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        attr_set = 1;
-    }
+    // per call (per device, thread safe; microseconds next to the kernel)
+    cudaFuncSetAttribute(schur32_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warp_schur_smem(32));
+    const int sms = device_sms();
     int per_sm = blocks_per_sm;
     if (per_sm <= 0) {
         per_sm = 1;
@@ -511,7 +510,7 @@ long long warp_schur_blocks(int n, long long N, int blocks_per_sm)
         if (per_sm < 1) per_sm = 1;
     }
     const long long need = (N + kWarpSchurThreads / 32 - 1) / (kWarpSchurThreads / 32);
-    return std::max<long long>(1, std::min<long long>(need, (long long)std::max(sms, 1) * per_sm));
+    return std::max<long long>(1, std::min<long long>(need, (long long)sms * per_sm));
 }
 
 }  // namespace

@@ -44,18 +44,14 @@ cudaError_t launch_persistent(int M, int N, int K, const __nv_bfloat16 *a, int l
                               const float *bias, int act, __nv_bfloat16 *c, float *cf, int ldc, int *err,
                               cudaStream_t st)
 {
-    static int max_smem_set = -1, sms = 0;  // per process: one device's attributes (the GB300's)
     const int smem = (tc::kM + NT) * K * 2;
-    if (max_smem_set < 0) {
-        const int cap = (tc::kM + NT) * 256 * 2;
-        cudaError_t e = cudaFuncSetAttribute(tc::gemm_bf16_persistent_kernel<NT>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-        if (e != cudaSuccess) return e;
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        max_smem_set = cap;
-    }
+    // per call (per device, thread safe; microseconds next to the kernel)
+    cudaError_t e = cudaFuncSetAttribute(tc::gemm_bf16_persistent_kernel<NT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (tc::kM + NT) * 256 * 2);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     constexpr int kCols = NT <= 32 ? 32 : (NT <= 64 ? 64 : (NT <= 128 ? 128 : 256));
     const int per_sm = std::max(1, std::min(512 / kCols, (220 * 1024) / smem));
     const int mtiles = (M + tc::kM - 1) / tc::kM;
@@ -553,13 +549,21 @@ cudaError_t forward(const ves_shiftnet *t, int rows, const ves::bf16 *X, const A
     return cudaGetLastError();
 }
 
+// Record a message for ves_last_error() and return the code.
+int fail(int code, const char *msg)
+{
+    ves::set_error_message(msg);
+    return code;
+}
+
 int create_from_config(ves_shiftnet **out, const ves_shiftnet_config &c)
 {
-    if (!out || !config_ok(c)) return VES_ERR_ARG;
+    ves::set_error_message("");
+    if (!out || !config_ok(c)) return fail(VES_ERR_ARG, "shiftnet: bad configuration");
     ves_shiftnet *t = new ves_shiftnet();
     cudaGetDevice(&t->dev);
     set_geometry(t, c);
-    if (!net_alloc(t)) { net_free(t); delete t; return VES_ERR_NOMEM; }
+    if (!net_alloc(t)) { net_free(t); delete t; return fail(VES_ERR_NOMEM, "shiftnet: device allocation failed"); }
     // He-style initialisation from a fixed seed (host), zero biases, identity normalisation
     std::mt19937_64 rng(c.seed);
     std::normal_distribution<float> nd(0.f, 1.f);
@@ -579,7 +583,7 @@ int create_from_config(ves_shiftnet **out, const ves_shiftnet_config &c)
     cudaMemcpy(t->fstd, one.data(), t->kin_pad * 4, cudaMemcpyHostToDevice);
     cudaMemcpy(t->tmean, zero.data(), t->nout_pad * 4, cudaMemcpyHostToDevice);
     cudaMemcpy(t->tstd, one.data(), t->nout_pad * 4, cudaMemcpyHostToDevice);
-    if (cudaDeviceSynchronize() != cudaSuccess) { net_free(t); delete t; return VES_ERR_CUDA; }
+    if (cudaDeviceSynchronize() != cudaSuccess) { net_free(t); delete t; return fail(VES_ERR_CUDA, "shiftnet: initialisation failed"); }
     *out = t;
     return VES_OK;
 }
@@ -603,7 +607,7 @@ void ves_shiftnet_default_config(ves_shiftnet_config *c)
 
 int ves_shiftnet_create_config(ves_shiftnet **out, const ves_shiftnet_config *cfg)
 {
-    if (!cfg) return VES_ERR_ARG;
+    if (!cfg) return fail(VES_ERR_ARG, "shiftnet: null configuration");
     return create_from_config(out, *cfg);
 }
 
@@ -631,8 +635,9 @@ int ves_shiftnet_train(ves_shiftnet *t, long long count, int thread_cnt, const d
 {
     if (!t || count < 1 || count > 0x7fffffffLL || thread_cnt < 1 || (count % thread_cnt) || !rA || !iA || !rE ||
         !iE || epochs < 0 || batch < 32 || batch > 65536 || !(lr > 0.f))
-        return VES_ERR_ARG;
-    if (t->P > 0 && !params) return VES_ERR_ARG;
+        return fail(VES_ERR_ARG, "shiftnet train: bad arguments (count a multiple of thread_cnt, 32 <= batch <= 65536)");
+    if (t->P > 0 && !params) return fail(VES_ERR_ARG, "shiftnet train: the network needs family parameters");
+    ves::set_error_message("");
     cudaStream_t st = (cudaStream_t)stream;
     const int n = t->n, H = t->H, L = t->L;
     ves::bf16 *Xall = nullptr, *Xb = nullptr;
@@ -735,6 +740,8 @@ int ves_shiftnet_train(ves_shiftnet *t, long long count, int thread_cnt, const d
     cudaFree(Xall); cudaFree(Tall); cudaFree(Xb); cudaFree(Tb); cudaFree(dA); cudaFree(dB); cudaFree(loss);
     cudaFree(rows); cudaFree(err); cudaFree(actbuf);
     for (int l = 0; l <= L; ++l) { cudaFree(gW[l]); cudaFree(gb[l]); }
+    if (rc == VES_ERR_NOMEM) return fail(rc, "shiftnet train: device allocation failed");
+    if (rc != VES_OK) return fail(rc, "shiftnet train: a kernel failed or a tensor-core wait timed out");
     return rc;
 }
 
@@ -751,10 +758,12 @@ int ves_shiftnet_predict(const ves_shiftnet *t, long long count, int thread_cnt,
 {
     if (!t || count < 0 || count > 0x7fffffffLL || thread_cnt < 1 || (count % thread_cnt) || !rA || !iA || !rS ||
         !iS)
-        return VES_ERR_ARG;
-    if (t->P > 0 && !params) return VES_ERR_ARG;
+        return fail(VES_ERR_ARG, "shiftnet predict: bad arguments");
+    if (t->P > 0 && !params) return fail(VES_ERR_ARG, "shiftnet predict: the network needs family parameters");
+    ves::set_error_message("");
     if (count == 0) return VES_OK;
-    if (!workspace || workspace_bytes < ves_shiftnet_predict_workspace_size(t, count)) return VES_ERR_ARG;
+    if (!workspace || workspace_bytes < ves_shiftnet_predict_workspace_size(t, count))
+        return fail(VES_ERR_ARG, "shiftnet predict: workspace missing or too small");
     cudaStream_t st = (cudaStream_t)stream;
     char *w = static_cast<char *>(workspace);
     ves::bf16 *X = reinterpret_cast<ves::bf16 *>(w);
@@ -763,7 +772,7 @@ int ves_shiftnet_predict(const ves_shiftnet *t, long long count, int thread_cnt,
     int *err = nullptr;  // a GEMM wait that gives up leaves its tile unwritten; training checks the flag
     ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, t->n, t->P, t->F, thread_cnt, params, rA, iA,
                                                          t->fmean, t->fstd, t->kin, t->kin_pad, X, nullptr);
-    if (forward(t, (int)count, X, a, err, st, false) != cudaSuccess) return VES_ERR_CUDA;
+    if (forward(t, (int)count, X, a, err, st, false) != cudaSuccess) return fail(VES_ERR_CUDA, "shiftnet predict: launch failed");
     ves::shifts_out_kernel<<<ves::nb(count), 256, 0, st>>>(count, t->n, thread_cnt, t->nout_pad, a.Y, t->tmean,
                                                            t->tstd, rS, iS);
     return cudaGetLastError() == cudaSuccess ? VES_OK : VES_ERR_CUDA;
@@ -774,9 +783,9 @@ int ves_shiftnet_predict(const ves_shiftnet *t, long long count, int thread_cnt,
 // normalisation vectors.
 int ves_shiftnet_save(const ves_shiftnet *t, const char *path)
 {
-    if (!t || !path) return VES_ERR_ARG;
+    if (!t || !path) return fail(VES_ERR_ARG, "shiftnet save: null argument");
     FILE *f = fopen(path, "wb");
-    if (!f) return VES_ERR_ARG;
+    if (!f) return fail(VES_ERR_ARG, "shiftnet save: cannot open the file");
     const int hdr[9] = {0x56455353, 2, t->n, t->P, t->H, t->L, t->F, t->cfg.loss, (int)t->step};
     bool ok = fwrite(hdr, sizeof hdr, 1, f) == 1 && fwrite(&t->cfg.delta, 4, 1, f) == 1 &&
               fwrite(&t->cfg.seed, 8, 1, f) == 1;
@@ -796,16 +805,16 @@ int ves_shiftnet_save(const ves_shiftnet *t, const char *path)
 
 int ves_shiftnet_load(ves_shiftnet **out, const char *path)
 {
-    if (!out || !path) return VES_ERR_ARG;
+    if (!out || !path) return fail(VES_ERR_ARG, "shiftnet load: null argument");
     FILE *f = fopen(path, "rb");
-    if (!f) return VES_ERR_ARG;
+    if (!f) return fail(VES_ERR_ARG, "shiftnet load: cannot open the file");
     int hdr[9];
     ves_shiftnet_config c;
     ves_shiftnet_default_config(&c);
     if (fread(hdr, sizeof hdr, 1, f) != 1 || hdr[0] != 0x56455353 || hdr[1] != 2 || fread(&c.delta, 4, 1, f) != 1 ||
         fread(&c.seed, 8, 1, f) != 1) {
         fclose(f);
-        return VES_ERR_ARG;
+        return fail(VES_ERR_ARG, "shiftnet load: not a version-2 shift network checkpoint");
     }
     c.dim = hdr[2]; c.n_params = hdr[3]; c.hidden = hdr[4]; c.layers = hdr[5]; c.fourier = hdr[6]; c.loss = hdr[7];
     ves_shiftnet *t = nullptr;
@@ -826,7 +835,10 @@ int ves_shiftnet_load(ves_shiftnet **out, const char *path)
     }
     get(t->fmean, t->kin_pad); get(t->fstd, t->kin_pad); get(t->tmean, t->nout_pad); get(t->tstd, t->nout_pad);
     fclose(f);
-    if (!ok || cudaDeviceSynchronize() != cudaSuccess) { ves_shiftnet_destroy(t); return VES_ERR_CUDA; }
+    if (!ok || cudaDeviceSynchronize() != cudaSuccess) {
+        ves_shiftnet_destroy(t);
+        return fail(VES_ERR_CUDA, "shiftnet load: truncated file or device error");
+    }
     *out = t;
     return VES_OK;
 }
