@@ -87,10 +87,16 @@ def test_fullsize_gauss8_all_vs_oracle():
 def test_fullsize_varsize_families():
     """500,000 matrices of orders 4..64 (Gaussian / non-normal / clustered,
     seed 2) in one mixed-size solve: every residual on the device; the first
-    3,000 matrices against the oracle.  Eigenvalue agreement is held to
-    1e-12 ||A||_F except for the non-normal family, whose eigenvalues have
-    condition numbers up to cond(V) = 1e4: two backward-stable solvers may then
-    differ by up to cond(V) times that bar."""
+    3,000 matrices against LAPACK (numpy) and the oracle.
+
+    Bars: 1e-12 ||A||_F against LAPACK for the Gaussian and clustered
+    families; the non-normal family's eigenvalues have condition numbers up to
+    cond(V) = 1e4, so two backward-stable solvers may differ by up to that
+    factor more.  Against the oracle the same bars hold wherever the oracle
+    agrees with LAPACK: at orders up to 64 the reference's zgehrd reflector
+    sign (sign(Re alpha), which cancels in alpha - beta on columns that are
+    already nearly reduced) costs the oracle itself up to ~1e-9 on a few
+    matrices; those are reported, not held against the GPU."""
     import torch
     N = 500_000
     sizes, by_n = workloads.mixed_families(N, seed=2, device="cuda", as_list=False)
@@ -112,10 +118,12 @@ def test_fullsize_varsize_families():
         r = torch.linalg.vector_norm(A @ V - V * E[:, None, :], dim=1)
         q = r / (torch.linalg.matrix_norm(A)[:, None] * torch.linalg.vector_norm(V, dim=1))
         assert float(q.max()) <= 1e-13, (n, float(q.max()))
-    # oracle on the first 3,000 matrices, one SoA batch per order
     sub = 3000
     fam = np.arange(sub) % 3
-    worst = {0: 0.0, 1: 0.0, 2: 0.0}
+    bar = {0: 1e-12, 1: 1e-12 * 1e4, 2: 1e-12}
+    gl = {0: 0.0, 1: 0.0, 2: 0.0}   # GPU vs LAPACK
+    go = {0: 0.0, 1: 0.0, 2: 0.0}   # GPU vs oracle where the oracle agrees with LAPACK
+    oracle_off = 0                  # matrices where the oracle itself misses LAPACK's bar
     rh, ih = re.cpu().numpy(), im.cpu().numpy()
     erh, eih = er.cpu().numpy(), ei.cpu().numpy()
     for n in np.unique(sizes[:sub]):
@@ -125,13 +133,25 @@ def test_fullsize_varsize_families():
         ra, ia = ves.soa_from_complex(A, 1)
         rE, iE, *_ = oracle.eigensolve(ra, ia, int(n), 1)
         Eo = ves.complex_vec_from_soa(rE, iE, int(n), 1)
-        _, err, _ = match_eigs(Eg, Eo)
-        rel = (err / np.linalg.norm(A, axis=(1, 2))[:, None]).max(axis=1)
+        El = np.linalg.eigvals(A)
+        nA = np.linalg.norm(A, axis=(1, 2))
+        e_gl = (match_eigs(Eg, El)[1] / nA[:, None]).max(axis=1)
+        e_ol = (match_eigs(Eo, El)[1] / nA[:, None]).max(axis=1)
+        e_go = (match_eigs(Eg, Eo)[1] / nA[:, None]).max(axis=1)
         for f in (0, 1, 2):
-            if (fam[ids] == f).any():
-                worst[f] = max(worst[f], float(rel[fam[ids] == f].max()))
-    assert worst[0] <= 1e-12 and worst[2] <= 1e-12, worst
-    assert worst[1] <= 1e-12 * 1e4, worst
+            sel = fam[ids] == f
+            if not sel.any():
+                continue
+            gl[f] = max(gl[f], float(e_gl[sel].max()))
+            good = sel & (e_ol <= bar[f])
+            oracle_off += int((sel & ~good).sum())
+            if good.any():
+                go[f] = max(go[f], float(e_go[good].max()))
+    print("GPU vs LAPACK", gl, "GPU vs oracle (oracle accurate)", go, "oracle off LAPACK:", oracle_off)
+    for f in (0, 1, 2):
+        assert gl[f] <= bar[f], (f, gl)
+        assert go[f] <= bar[f], (f, go)
+    assert oracle_off <= sub // 100
 
 
 def test_fullsize_learned_config():
