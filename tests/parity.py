@@ -5,15 +5,20 @@ from scipy.optimize import linear_sum_assignment
 
 
 def match_eigs(E, Eref):
-    """Per matrix, the permutation p minimising max |E[p] - Eref| (identity
-    when the orders already agree).  Returns (perm (N, n), err (N,) = max
-    matched |E - Eref|, same_order (N,) bool)."""
+    """Per matrix, the optimal assignment p of E to Eref (minimum total
+    |E[p] - Eref|, Hungarian), unless the given orders already agree to
+    1e-13 of the spectrum's scale.  Returns (perm (N, n), err (N,) = max
+    matched |E - Eref|, same_order (N,) bool: the orders agree to 1e-8, i.e.
+    the same Schur order).  Accepting an order at a looser tolerance would
+    report the separation of two close eigenvalues listed in swapped order as
+    an error."""
     N, n = E.shape
     perm = np.tile(np.arange(n), (N, 1))
     d0 = np.abs(E - Eref)
     scale = np.maximum(np.abs(Eref).max(axis=1, keepdims=True), 1e-300)
     same = (d0 <= 1e-8 * scale).all(axis=1)
-    for k in np.nonzero(~same)[0]:
+    exact = (d0 <= 1e-13 * scale).all(axis=1)
+    for k in np.nonzero(~exact)[0]:
         C = np.abs(E[k][:, None] - Eref[k][None, :])
         r, c = linear_sum_assignment(C)
         p = np.empty(n, dtype=int)
