@@ -188,3 +188,28 @@ def test_mixed_schur_kernels(n, mode, monkeypatch):
     assert (err / nA).max() <= 1e-12, (err / nA).max()
     assert residuals(A, out["E"], out["V"]).max() <= 1e-13
     assert (out["status"] & ~ves.VES_STATUS_REFINE_FALLBACK == 0).all()
+
+
+@pytest.mark.parametrize("n,N", [(8, 50688), (24, 33280)])
+def test_mixed_overlap_equals_serial(n, N, monkeypatch):
+    """The FP32+refine form cuts large batches into chunks and overlaps one
+    chunk's Schur stage with the previous chunk's refinement on two streams;
+    the results equal the serial launch order bit for bit (n = 8: the lane
+    Schur kernel, n = 24: the warp one; unequal last chunk)."""
+    import torch
+    tc = 512
+    rA, iA = workloads.gaussian_soa(N, n, 17, tc)
+    dA = [torch.from_numpy(x).cuda() for x in (rA, iA)]
+    outs = []
+    for ov in ("1", "0"):
+        monkeypatch.setenv("VES_MIXED_OVERLAP", ov)
+        dE = [torch.empty(N * n, dtype=torch.float64, device="cuda") for _ in range(2)]
+        dV = [torch.empty_like(dA[0]) for _ in range(2)]
+        st = torch.full((N,), -1, dtype=torch.int32, device="cuda")
+        ves.eigensolve(n, N // tc, tc, dA[0], dA[1], dE[0], dE[1], dV[0], dV[1], status=st,
+                       options=ves.default_options(precision=MIX))
+        torch.cuda.synchronize()
+        outs.append([t.cpu().numpy() for t in dE + dV + [st]])
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a, b)
+    assert ((outs[0][4] & ~ves.VES_STATUS_REFINE_FALLBACK) == 0).all()

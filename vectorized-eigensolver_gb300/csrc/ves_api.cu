@@ -157,6 +157,25 @@ WsPlan workspace_plan(int precision, int n, long long N, bool vectors, int bps)
 // ---------------------------------------------------------------------------
 // Drop-in bodies (bool: success).
 // ---------------------------------------------------------------------------
+// Streams the asynchronous entry points fork work onto (the FP32+refine form's
+// Schur / refinement overlap), two per device, created on first use; work on
+// them is always ordered after and joined back into the caller's stream.
+cudaStream_t library_stream(int k)
+{
+    static std::mutex mu;
+    static std::vector<std::array<cudaStream_t, 2>> streams;  // [device][k]
+    int d = 0;
+    if (cudaGetDevice(&d) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lk(mu);
+    if ((int)streams.size() <= d) streams.resize(d + 1, std::array<cudaStream_t, 2>{nullptr, nullptr});
+    cudaStream_t &st = streams[d][k];
+    if (!st && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        st = nullptr;
+    }
+    return st;
+}
+
 // Streams of the drop-in eigensolver's copy/solve pipeline, created once per
 // device (called with the pool mutex held).
 cudaStream_t pipeline_stream(int k)
@@ -596,7 +615,18 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
     m.fb_list = list;
     m.fb_count = count;
     m.blocks_per_sm = o.blocks_per_sm;
-    if (!cuda_ok(ves::launch_mixed(m, st), "mixed-precision kernel launch")) return VES_ERR_CUDA;
+    // The Schur stage of one chunk overlaps the refinement of the previous one on
+    // two library streams (forked from and joined back into the caller's);
+    // VES_MIXED_OVERLAP=0 runs the two stages one after the other on the caller's stream.
+    const char *ov = getenv("VES_MIXED_OVERLAP");
+    cudaStream_t s_schur = nullptr, s_refine = nullptr;
+    if (!(ov && ov[0] == '0')) {
+        s_schur = library_stream(0);
+        s_refine = library_stream(1);
+    }
+    const cudaError_t me = (s_schur && s_refine) ? ves::launch_mixed_overlap(m, st, s_schur, s_refine)
+                                                 : ves::launch_mixed(m, st);
+    if (!cuda_ok(me, "mixed-precision kernel launch")) return VES_ERR_CUDA;
     a.list = list;
     a.list_count = count;
     return native(cuda_ok(ves::launch_fused_fp64(a, st), "fallback kernel launch"));

@@ -57,10 +57,18 @@ struct MixedArgs {
     int *fb_list;   // matrices handed to the FP64 solver
     int *fb_count;
     int blocks_per_sm;  // FP32 Schur kernel grid: blocks per SM; 0 = default
+    // matrices [m_begin, m_end) of the batch (a multiple of 32 where a chunk
+    // ends inside the batch); launch_mixed sets the whole batch when m_end == 0
+    long long m_begin, m_end;
 };
 
 size_t mixed_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blocks, int *out_threads);
 cudaError_t launch_mixed(const MixedArgs &a, cudaStream_t st);
+// The same work with the batch cut into chunks: the FP32 Schur stage of a
+// chunk runs on s_schur while the previous chunk's FP64 refinement runs on
+// s_refine (the two kernels are bound by different units: latency of the FP32
+// sweeps, the FP64 pipe), forked from and joined back into `st`.
+cudaError_t launch_mixed_overlap(const MixedArgs &a, cudaStream_t st, cudaStream_t s_schur, cudaStream_t s_refine);
 
 // Fused zgehrd -> zunghr -> zlahqr -> ztrevc, FP64.
 // blocks_per_sm = 0 takes the library default (VES_FUSED_BLOCKS_PER_SM, else 2).

@@ -90,15 +90,15 @@ __global__ void __launch_bounds__(kSchurThreads) schur32_kernel(const MixedArgs 
     const int lane = threadIdx.x & 31;
     const long long warp = (long long)blockIdx.x * (kSchurThreads / 32) + (threadIdx.x >> 5);
     const long long nwarps = (long long)gridDim.x * (kSchurThreads / 32);
-    const long long ngroups = (N + 31) / 32;
+    const long long g_end = (a.m_end + 31) / 32;
     const long long nn = (long long)n * n;
-    for (long long g = warp; g < ngroups; g += nwarps) {
+    for (long long g = a.m_begin / 32 + warp; g < g_end; g += nwarps) {
         float2 *pT = buf + g * group_elems(n) * 32 + lane;
         float2 *pZ = pT + 32 * nn, *pX = pZ + 32 * nn, *pW = pX + 32 * nn;
         const MatIlv<float> T{pT, n}, Z{pZ, n};
         const VecIlv<float> W{pW};
         const long long m = g * 32 + lane;
-        const bool valid = m < N;
+        const bool valid = m >= a.m_begin && m < a.m_end;
         int status = 0, sweeps = 0;
         bool fb = false;
         float nA2 = 0.f;
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
     const float ulp = lim<float>::eps();
     const float smlnum = lim<float>::tiny() * ((float)n / ulp);
 
-    for (long long m = gw; m < N; m += nw) {
+    for (long long m = a.m_begin + gw; m < a.m_end; m += nw) {
         // ---- load A (FP64 SoA) into H as FP32; non-finite / out-of-range check
         const long long mo = soa_off_m(m, nn, tc);
         bool bad = false;
@@ -345,8 +345,8 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
 {
     const int n = a.g.n, tc = a.g.tc;
     const long long N = a.g.N;
-    const long long p = (long long)blockIdx.x * kRefineThreads + threadIdx.x;
-    const bool valid = p < N * n;
+    const long long p = a.m_begin * n + (long long)blockIdx.x * kRefineThreads + threadIdx.x;
+    const bool valid = p < a.m_end * n;
     const long long m = valid ? p / n : 0;
     const int k = valid ? (int)(p % n) + 1 : 1;
     bool act = valid && flags[m] == 0;
@@ -515,38 +515,126 @@ long long warp_schur_blocks(int n, long long N, int blocks_per_sm)
 
 }  // namespace
 
-cudaError_t launch_mixed(const MixedArgs &a, cudaStream_t st)
+namespace {
+
+struct MixedBufs {
+    float2 *buf;
+    int *flags;
+};
+MixedBufs mixed_bufs(const MixedArgs &a)
 {
-    if (a.g.N <= 0) return cudaSuccess;
-    const int n = a.g.n;
-    if (n > 64) return cudaErrorInvalidValue;  // the refinement keeps per-pair vectors of at most 64 entries
     const long long groups = (a.g.N + 31) / 32;
     float2 *buf = static_cast<float2 *>(a.ws);
     int *flags = reinterpret_cast<int *>(static_cast<char *>(a.ws) +
-                                         (size_t)groups * group_elems(n) * 32 * sizeof(float2));
-    const bool warp = use_warp_schur(n);
-    if (warp)
-        schur32_warp_kernel<<<(unsigned)warp_schur_blocks(n, a.g.N, a.blocks_per_sm), kWarpSchurThreads,
-                              warp_schur_smem(n), st>>>(a, buf, flags);
+                                         (size_t)groups * group_elems(a.g.n) * 32 * sizeof(float2));
+    return {buf, flags};
+}
+
+// FP32 Schur stage of matrices [a.m_begin, a.m_end)
+cudaError_t launch_schur(const MixedArgs &a, int blocks_per_sm, cudaStream_t st)
+{
+    const int n = a.g.n;
+    const long long cnt = a.m_end - a.m_begin;
+    const MixedBufs b = mixed_bufs(a);
+    if (use_warp_schur(n))
+        schur32_warp_kernel<<<(unsigned)warp_schur_blocks(n, cnt, blocks_per_sm), kWarpSchurThreads,
+                              warp_schur_smem(n), st>>>(a, b.buf, b.flags);
     else
-        schur32_kernel<<<(unsigned)schur_blocks(a.g.N, a.blocks_per_sm), kSchurThreads, 0, st>>>(a, buf, flags);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    const long long pairs = a.g.N * n;
+        schur32_kernel<<<(unsigned)schur_blocks(cnt, blocks_per_sm), kSchurThreads, 0, st>>>(a, b.buf, b.flags);
+    return cudaGetLastError();
+}
+
+// FP64 refinement of the eigenpairs of matrices [a.m_begin, a.m_end)
+cudaError_t launch_refine(const MixedArgs &a, cudaStream_t st)
+{
+    const int n = a.g.n;
+    const MixedBufs b = mixed_bufs(a);
+    const long long pairs = (a.m_end - a.m_begin) * n;
     const unsigned rb = (unsigned)((pairs + kRefineThreads - 1) / kRefineThreads);
-    if (warp) {
+    if (use_warp_schur(n)) {
         if (n <= 16)
-            refine_kernel<16, true><<<rb, kRefineThreads, 0, st>>>(a, buf, flags);
+            refine_kernel<16, true><<<rb, kRefineThreads, 0, st>>>(a, b.buf, b.flags);
         else
-            refine_kernel<32, true><<<rb, kRefineThreads, 0, st>>>(a, buf, flags);
+            refine_kernel<32, true><<<rb, kRefineThreads, 0, st>>>(a, b.buf, b.flags);
     } else if (n <= 16) {
-        refine_kernel<16, false><<<rb, kRefineThreads, 0, st>>>(a, buf, flags);
+        refine_kernel<16, false><<<rb, kRefineThreads, 0, st>>>(a, b.buf, b.flags);
     } else if (n <= 32) {
-        refine_kernel<32, false><<<rb, kRefineThreads, 0, st>>>(a, buf, flags);
+        refine_kernel<32, false><<<rb, kRefineThreads, 0, st>>>(a, b.buf, b.flags);
     } else {
-        refine_kernel<64, false><<<rb, kRefineThreads, 0, st>>>(a, buf, flags);
+        refine_kernel<64, false><<<rb, kRefineThreads, 0, st>>>(a, b.buf, b.flags);
     }
     return cudaGetLastError();
+}
+
+MixedArgs whole_batch(const MixedArgs &a)
+{
+    MixedArgs w = a;
+    if (w.m_end <= 0) {
+        w.m_begin = 0;
+        w.m_end = a.g.N;
+    }
+    return w;
+}
+
+}  // namespace
+
+cudaError_t launch_mixed(const MixedArgs &a0, cudaStream_t st)
+{
+    if (a0.g.N <= 0) return cudaSuccess;
+    if (a0.g.n > 64) return cudaErrorInvalidValue;  // the refinement keeps per-pair vectors of at most 64 entries
+    const MixedArgs a = whole_batch(a0);
+    cudaError_t e = launch_schur(a, a.blocks_per_sm, st);
+    if (e != cudaSuccess) return e;
+    return launch_refine(a, st);
+}
+
+cudaError_t launch_mixed_overlap(const MixedArgs &a0, cudaStream_t st, cudaStream_t s_schur, cudaStream_t s_refine)
+{
+    if (a0.g.N <= 0) return cudaSuccess;
+    if (a0.g.n > 64) return cudaErrorInvalidValue;
+    const MixedArgs a = whole_batch(a0);
+    const long long N = a.m_end - a.m_begin;
+    // chunks of whole 512-matrix units, at most 8; each chunk keeps the GPU busy on its own
+    const long long unit = 512;
+    long long nch = std::min<long long>(8, std::max<long long>(1, N / (32 * unit)));
+    long long csz = ((N + nch - 1) / nch + unit - 1) / unit * unit;
+    nch = (N + csz - 1) / csz;
+    if (nch < 2) return launch_mixed(a, st);
+    // the Schur kernel leaves room on each SM for refinement blocks (default 4
+    // blocks per SM; VES_MIXED_OVERLAP_BLOCKS_PER_SM overrides)
+    int bps = a.blocks_per_sm > 0 ? a.blocks_per_sm : 4;
+    if (a.blocks_per_sm <= 0)
+        if (const char *ev = getenv("VES_MIXED_OVERLAP_BLOCKS_PER_SM")) {
+            const int v = atoi(ev);
+            if (v >= 1 && v <= 16) bps = v;
+        }
+    cudaEvent_t fork = nullptr, join_s = nullptr, join_r = nullptr;
+    cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join_s, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join_r, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(fork, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s_schur, fork, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s_refine, fork, 0);
+    for (long long c = 0; c < nch && e == cudaSuccess; ++c) {
+        MixedArgs ch = a;
+        ch.m_begin = a.m_begin + c * csz;
+        ch.m_end = std::min(a.m_end, ch.m_begin + csz);
+        cudaEvent_t done = nullptr;
+        e = launch_schur(ch, bps, s_schur);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(done, s_schur);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s_refine, done, 0);
+        if (e == cudaSuccess) e = launch_refine(ch, s_refine);
+        if (done) cudaEventDestroy(done);  // released once the device has passed it
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(join_s, s_schur);
+    if (e == cudaSuccess) e = cudaEventRecord(join_r, s_refine);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, join_s, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, join_r, 0);
+    if (fork) cudaEventDestroy(fork);
+    if (join_s) cudaEventDestroy(join_s);
+    if (join_r) cudaEventDestroy(join_r);
+    return e;
 }
 
 }  // namespace ves
