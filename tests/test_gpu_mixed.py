@@ -108,7 +108,7 @@ def test_mixed_clustered_spectrum():
     out = run_fused(A, 32, precision=MIX)
     assert residuals(A, out["E"], out["V"]).max() <= 1e-13
     _, err, _ = match_eigs(out["E"], oracle_E(A, 32))
-    assert (err / np.linalg.norm(A, axis=(1, 2))).max() <= 1e-9  # the oracle itself is only this accurate here
+    assert (err / np.linalg.norm(A, axis=(1, 2))).max() <= 1e-12
 
 
 @pytest.mark.parametrize("vnorm", [0, 2])

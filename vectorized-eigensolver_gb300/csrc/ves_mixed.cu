@@ -600,9 +600,12 @@ cudaError_t launch_mixed_overlap(const MixedArgs &a0, cudaStream_t st, cudaStrea
     long long csz = ((N + nch - 1) / nch + unit - 1) / unit * unit;
     nch = (N + csz - 1) / csz;
     if (nch < 2) return launch_mixed(a, st);
-    // the Schur kernel leaves room on each SM for refinement blocks (default 4
-    // blocks per SM; VES_MIXED_OVERLAP_BLOCKS_PER_SM overrides)
-    int bps = a.blocks_per_sm > 0 ? a.blocks_per_sm : 4;
+    // the Schur kernel leaves room on each SM for refinement blocks: 4 blocks
+    // per SM for the lane kernel, 6 for the warp kernel (measured on GB300,
+    // FP32+refine eigensolves/s serial -> overlapped: n=8 36.1 -> 41.0 M/s,
+    // n=16 5.10 -> 5.87 M/s, n=24 1.63 -> 1.72 M/s, n=32 0.726 -> 0.846 M/s);
+    // VES_MIXED_OVERLAP_BLOCKS_PER_SM overrides
+    int bps = a.blocks_per_sm > 0 ? a.blocks_per_sm : (use_warp_schur(a.g.n) ? 6 : 4);
     if (a.blocks_per_sm <= 0)
         if (const char *ev = getenv("VES_MIXED_OVERLAP_BLOCKS_PER_SM")) {
             const int v = atoi(ev);
