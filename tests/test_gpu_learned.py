@@ -131,24 +131,3 @@ def test_polish_recovers_noisy_predictions(n):
     assert (err / nA).max() <= 1e-12
     assert sw.double().mean().item() < 0.8 * sw0.double().mean().item()
     assert ((st & ~ves.VES_STATUS_SHIFT_FALLBACK) == 0).all()
-
-
-def test_polish_overlap_equals_serial(monkeypatch):
-    """Large batches polish chunk c + 1 while chunk c is solved, on two
-    streams; the results equal pre-pass-then-solve bit for bit (two chunks of
-    67 and 66 blocks)."""
-    import torch
-    n, N = 16, 133 * TC
-    p, rA, iA = learned_shift.family(N, n, param_seed=15)
-    rE0, iE0, _ = learned_shift.solve_plain(n, N, rA, iA, TC)
-    g = torch.Generator(device="cuda").manual_seed(2)
-    rS = rE0 + 1e-2 * torch.randn(rE0.shape, generator=g, device="cuda", dtype=torch.float64)
-    iS = iE0 + 1e-2 * torch.randn(rE0.shape, generator=g, device="cuda", dtype=torch.float64)
-    outs = []
-    for ov in ("1", "0"):
-        monkeypatch.setenv("VES_SHIFTS_OVERLAP", ov)
-        rE, iE, st, sw, fb, res = solve_shifts(n, N, rA, iA, rS, iS, shift_polish=4, shift_gate=3e-2)
-        assert res <= 1e-13
-        outs.append([t.cpu().numpy() for t in (rE, iE, st, sw, fb)])
-    for a, b in zip(*outs):
-        np.testing.assert_array_equal(a, b)

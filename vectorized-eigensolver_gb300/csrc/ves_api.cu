@@ -781,67 +781,11 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *
         // n <= 32: polish in a warp-per-matrix FP32 pre-pass, the solve reads the result
         double *rP = reinterpret_cast<double *>(static_cast<char *>(ws) + plan.fused);
         double *iP = rP + (size_t)g.N * dim;
+        if (!cuda_ok(ves::launch_polish32(g, rA, iA, rS, iS, rP, iP, o.shift_polish, st), "shift polish launch"))
+            return VES_ERR_CUDA;
         a.rS = rP;
         a.iS = iP;
         a.shift_polish = 0;
-        // Large batches: chunks of whole SoA blocks (contiguous in every plane);
-        // the polish of chunk c + 1 runs on one library stream while chunk c is
-        // solved on the other (FP32 / shared-memory work beside the FP64-bound
-        // solve).  VES_SHIFTS_OVERLAP=0 runs pre-pass and solve in sequence.
-        const char *ov = getenv("VES_SHIFTS_OVERLAP");
-        const long long nch0 = std::min<long long>(std::min<long long>(8, g.N / 32768), block_cnt);
-        cudaStream_t s1 = nullptr, s2 = nullptr;
-        if (nch0 >= 2 && !(ov && ov[0] == '0')) {
-            s1 = library_stream(0);
-            s2 = library_stream(1);
-        }
-        if (!s1 || !s2) {
-            if (!cuda_ok(ves::launch_polish32(g, rA, iA, rS, iS, rP, iP, o.shift_polish, st), "shift polish launch"))
-                return VES_ERR_CUDA;
-            return native(cuda_ok(ves::launch_fused_fp64(a, st), "learned-shift solve launch"));
-        }
-        const long long cb = (block_cnt + nch0 - 1) / nch0;  // blocks per chunk
-        const long long nch = (block_cnt + cb - 1) / cb;
-        const size_t mstride = (size_t)thread_cnt * dim * dim, vstride = (size_t)thread_cnt * dim;
-        std::vector<cudaEvent_t> evs;
-        auto event = [&]() -> cudaEvent_t {
-            cudaEvent_t e = nullptr;
-            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
-            evs.push_back(e);
-            return e;
-        };
-        cudaError_t e = cudaSuccess;
-        cudaEvent_t fork = event();
-        e = fork ? cudaEventRecord(fork, st) : cudaErrorMemoryAllocation;
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(s1, fork, 0);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, fork, 0);
-        for (long long c = 0; c < nch && e == cudaSuccess; ++c) {
-            const long long b0 = c * cb, nb = std::min<long long>(cb, block_cnt - b0);
-            const size_t mo = b0 * mstride, vo = b0 * vstride;
-            const long long m0 = b0 * thread_cnt;
-            const ves::Geom gc{dim, nb * (long long)thread_cnt, thread_cnt};
-            e = ves::launch_polish32(gc, rA + mo, iA + mo, rS + vo, iS + vo, rP + vo, iP + vo, o.shift_polish, s1);
-            cudaEvent_t done = e == cudaSuccess ? event() : nullptr;
-            if (e == cudaSuccess) e = done ? cudaEventRecord(done, s1) : cudaErrorMemoryAllocation;
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, done, 0);
-            ves::FusedArgs ac = a;
-            ac.g = gc;
-            ac.rA = rA + mo; ac.iA = iA + mo;
-            ac.rE = rE + vo; ac.iE = iE + vo;
-            ac.rV = rV + mo; ac.iV = iV + mo;
-            ac.rS = rP + vo; ac.iS = iP + vo;
-            ac.status = status ? status + m0 : nullptr;
-            ac.sweeps = sweeps ? sweeps + m0 : nullptr;
-            ac.fallbacks = fallbacks ? fallbacks + m0 : nullptr;
-            if (e == cudaSuccess) e = ves::launch_fused_fp64(ac, s2);
-        }
-        cudaEvent_t j1 = e == cudaSuccess ? event() : nullptr, j2 = e == cudaSuccess ? event() : nullptr;
-        if (e == cudaSuccess) e = (j1 && j2) ? cudaEventRecord(j1, s1) : cudaErrorMemoryAllocation;
-        if (e == cudaSuccess) e = cudaEventRecord(j2, s2);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, j1, 0);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, j2, 0);
-        for (cudaEvent_t ev : evs) cudaEventDestroy(ev);  // released once the device has passed them
-        return native(cuda_ok(e, "learned-shift solve launch"));
     }
     return native(cuda_ok(ves::launch_fused_fp64(a, st), "learned-shift solve launch"));
 }
