@@ -156,9 +156,13 @@ size_t ves_eigensolve_workspace_size(int dim, int block_cnt, int thread_cnt, con
  * (nullable, may alias rA/iA) receive the Schur form.  status and sweeps
  * (nullable) receive one int per matrix: VES_STATUS_* bits and the number of
  * QR sweeps.  workspace may be NULL (the library then uses a cached
- * allocation of its own, grown on demand and held until ves_release()),
- * otherwise it must hold ves_eigensolve_workspace_size() bytes, 256-byte
- * aligned.  Asynchronous on `stream`. */
+ * allocation of its own, grown on demand and held until ves_release(); it is
+ * shared by every call on the device, so calls that can run at the same time
+ * on different streams must each pass their own workspace), otherwise it must
+ * hold ves_eigensolve_workspace_size() bytes, 256-byte aligned.  Asynchronous
+ * on `stream`; for large batches the FP32 + refinement form runs on two
+ * library streams forked from `stream` by an event and joined back into it
+ * (VES_MIXED_OVERLAP=0 in the environment keeps everything on `stream`). */
 int ves_eigensolve(int dim, int block_cnt, int thread_cnt,
                    const double *rA, const double *iA, double *rE, double *iE, double *rV, double *iV,
                    double *rT, double *iT, int *status, int *sweeps,
