@@ -571,19 +571,24 @@ def run_gpu_arm(args, d):
                          % (sample, reps, tot, cores)}
 
     forms = []
+    want = set(args.forms.split(",")) if args.forms else {"mixed16", "n32", "learned", "varsize"}
     if d.world == 1 and not args.no_forms:
-        forms.append(dict(measure_form("FP32+refine", n, N, w["seed"], tc, 1, 2, args.steps),
-                          speedup_vs_plain=None))
-        forms[-1]["speedup_vs_plain"] = forms[-1]["value"] / value
-        p32 = measure_form("plain FP64", 32, 262_144, 3, 512, 0, 1, 2)
-        m32 = measure_form("FP32+refine", 32, 262_144, 3, 512, 1, 1, 2)
-        m32["speedup_vs_plain"] = m32["value"] / p32["value"]
-        forms += [p32, m32]
-        for ln in (16, 32):
-            log("[bench] learned-shift form, n=%d" % ln)
-            forms.append(measure_learned(ln, 262_144, 200_000, 2))
-        log("[bench] mixed-size form")
-        forms.append(measure_varsize(500_000, 2))
+        if "mixed16" in want:
+            forms.append(dict(measure_form("FP32+refine", n, N, w["seed"], tc, 1, 2, args.steps),
+                              speedup_vs_plain=None))
+            forms[-1]["speedup_vs_plain"] = forms[-1]["value"] / value
+        if "n32" in want:
+            p32 = measure_form("plain FP64", 32, 262_144, 3, 512, 0, 1, 2)
+            m32 = measure_form("FP32+refine", 32, 262_144, 3, 512, 1, 1, 2)
+            m32["speedup_vs_plain"] = m32["value"] / p32["value"]
+            forms += [p32, m32]
+        if "learned" in want:
+            for ln in (16, 32):
+                log("[bench] learned-shift form, n=%d" % ln)
+                forms.append(measure_learned(ln, 262_144, 200_000, 2))
+        if "varsize" in want:
+            log("[bench] mixed-size form")
+            forms.append(measure_varsize(500_000, 2))
 
     d.done()
     if d.rank != 0:
@@ -732,6 +737,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the FP32+refine, n=32, learned-shift and mixed-size lines")
+    ap.add_argument("--forms", default="",
+                    help="comma list of the form lines to measure: mixed16, n32, learned, varsize (default all)")
     ap.add_argument("--ncu-case", type=int, default=0, metavar="N",
                     help="no benchmark: one solve per form on N matrices (for ncu captures)")
     ap.add_argument("--ncu-n", type=int, default=16)
