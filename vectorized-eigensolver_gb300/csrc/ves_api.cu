@@ -22,6 +22,31 @@
 #include <string>
 #include <vector>
 
+namespace ves {
+
+void load_kernels()
+{
+    static std::mutex mu;
+    static std::vector<char> done;  // [device]
+    int d = 0;
+    if (cudaGetDevice(&d) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    if ((int)done.size() <= d) done.resize(d + 1, 0);
+    if (done[d]) return;
+    done[d] = 1;
+    load_mixed_kernels();
+    load_fused_kernels();
+    load_varsize_kernels();
+    load_extras_kernels();
+    load_shiftnet_kernels();
+    cudaGetLastError();  // a failed load shows again, with its cause, at the launch
+}
+
+}  // namespace ves
+
 namespace {
 
 constexpr int kMaxDim = 512;
@@ -36,6 +61,14 @@ void set_error(const char *fmt, ...)
     vsnprintf(buf, sizeof buf, fmt, ap);
     va_end(ap);
     t_last_error = buf;
+}
+
+// Start of every entry point that launches work: clear the calling thread's
+// message and load the library's kernels on the current device (once).
+void begin_call()
+{
+    t_last_error.clear();
+    ves::load_kernels();
 }
 
 // Drop-in layer failures go to stderr as well: the reference API returns void.
@@ -403,7 +436,7 @@ bool do_backsubs(int dim, int bc, int tc, double *rT, double *iT, double *rb, do
 template <class F>
 void dropin(const char *name, F f)
 {
-    t_last_error.clear();
+    begin_call();
     if (!f()) report(name);
 }
 
@@ -528,7 +561,7 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
                    double *rV, double *iV, double *rT, double *iT, int *status, int *sweeps, const ves_options *opt,
                    void *workspace, size_t workspace_bytes, void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     ves::Geom g;
     if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
     if (g.N == 0) return VES_OK;
@@ -642,7 +675,7 @@ size_t ves_polyroots_workspace_size(int degree, int block_cnt, int thread_cnt)
 int ves_polyroots(int degree, int block_cnt, int thread_cnt, const double *rC, const double *iC, double *rR,
                   double *iR, int *status, void *workspace, size_t workspace_bytes, void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     ves::Geom g;
     if (!geom_ok(degree, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
     if (g.N == 0) return VES_OK;
@@ -666,7 +699,7 @@ static int transpose_call(bool to_soa, bool vec, int dim, int block_cnt, int thr
                           const double *im_in, double *re_out, double *im_out, const void *z_in, void *z_out,
                           int row_major, void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     ves::Geom g;
     if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
     if (g.N == 0) return VES_OK;
@@ -736,7 +769,7 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *
                           int *sweeps, int *fallbacks, const ves_options *opt, void *workspace,
                           size_t workspace_bytes, void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     ves::Geom g;
     if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
     if (dim > 64) { set_error("learned shifts support dim <= 64"); return VES_ERR_UNSUPPORTED; }
@@ -793,7 +826,7 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *
 int ves_gemm_bf16(int M, int N, int K, const void *A, int lda, const void *Bt, int ldb, const float *bias, int act,
                   void *C, float *Cf, int ldc, int *err, void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     if (M < 0 || N < 0 || K < 0 || (K & 7) || (lda & 7) || (ldb & 7) || lda < K || ldb < K || ldc < N ||
         act < 0 || act > 1) {
         set_error("gemm: bad sizes (K, lda, ldb must be multiples of 8, lda, ldb >= K, ldc >= N)");
@@ -845,7 +878,7 @@ int ves_eigensolve_varsize(long long count, int max_dim, const int *dims, const 
                            double *rE, double *iE, double *rV, double *iV, int *status, int *sweeps,
                            const ves_options *opt, void *workspace, size_t workspace_bytes, void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     ves_options o;
     ves_default_options(&o);
     if (opt) o = *opt;
@@ -881,7 +914,7 @@ int ves_graph_capture_varsize(ves_graph **out, long long count, int max_dim, con
                               const double *iA, double *rE, double *iE, double *rV, double *iV, int *status,
                               int *sweeps, const ves_options *opt, void *workspace, size_t workspace_bytes)
 {
-    t_last_error.clear();
+    begin_call();
     if (!out) { set_error("null pointer"); return VES_ERR_ARG; }
     *out = nullptr;
     ves_options o;
@@ -918,7 +951,7 @@ int ves_graph_capture_varsize(ves_graph **out, long long count, int max_dim, con
 
 int ves_graph_launch(ves_graph *graph, void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     if (!graph || !graph->exec) { set_error("null graph"); return VES_ERR_ARG; }
     return native(cuda_ok(cudaGraphLaunch(graph->exec, (cudaStream_t)stream), "graph launch"));
 }
@@ -933,7 +966,7 @@ void ves_graph_destroy(ves_graph *graph)
 
 int ves_zgehrd(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau, void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     ves::Geom g;
     if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
     return native(cuda_ok(ves::launch_zgehrd(g, rA, iA, rtau, itau, (cudaStream_t)stream), "zgehrd launch"));
@@ -942,7 +975,7 @@ int ves_zgehrd(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, d
 int ves_zunghr(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, const double *rtau, const double *itau,
                void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     ves::Geom g;
     if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
     return native(cuda_ok(ves::launch_zunghr(g, rA, iA, rtau, itau, (cudaStream_t)stream), "zunghr launch"));
@@ -951,7 +984,7 @@ int ves_zunghr(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, c
 int ves_hessenberg(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rQ, double *iQ,
                    double *rtau, double *itau, void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     ves::Geom g;
     if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
     return native(cuda_ok(ves::launch_hessenberg(g, rA, iA, rQ, iQ, rtau, itau, (cudaStream_t)stream), "hessenberg launch"));
@@ -960,7 +993,7 @@ int ves_hessenberg(int dim, int block_cnt, int thread_cnt, double *rA, double *i
 int ves_zlahqr(int dim, int block_cnt, int thread_cnt, double *rE, double *iE, double *rM, double *iM, double *rS,
                double *iS, int *status, int max_its, void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     ves::Geom g;
     if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
     if (max_its < 0 || max_its > 10000) { set_error("max_its=%d outside [0, 10000]", max_its); return VES_ERR_ARG; }
@@ -971,7 +1004,7 @@ int ves_zlahqr(int dim, int block_cnt, int thread_cnt, double *rE, double *iE, d
 int ves_ztrevc(int dim, int block_cnt, int thread_cnt, double *rT, double *iT, double *rR, double *iR, double *rwork,
                double *iwork, void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     ves::Geom g;
     if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
     return native(cuda_ok(ves::launch_ztrevc(g, rT, iT, rR, iR, rwork, iwork, (cudaStream_t)stream), "ztrevc launch"));
@@ -980,7 +1013,7 @@ int ves_ztrevc(int dim, int block_cnt, int thread_cnt, double *rT, double *iT, d
 int ves_zgemv(bool hermitian, int dim, int block_cnt, int thread_cnt, const double *rM, const double *iM,
               const double *rx, const double *ix, double *ry, double *iy, double rbeta, double ibeta, void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     ves::Geom g;
     if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
     return native(cuda_ok(ves::launch_zgemv(g, hermitian, rM, iM, rx, ix, rbeta, ibeta, ry, iy, (cudaStream_t)stream),
@@ -990,7 +1023,7 @@ int ves_zgemv(bool hermitian, int dim, int block_cnt, int thread_cnt, const doub
 int ves_backsubstitution(int dim, int block_cnt, int thread_cnt, const double *rT, const double *iT, double *rb,
                          double *ib, void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     ves::Geom g;
     if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
     return native(cuda_ok(ves::launch_backsubs(g, rT, iT, rb, ib, (cudaStream_t)stream), "backsubstitution launch"));
@@ -998,7 +1031,7 @@ int ves_backsubstitution(int dim, int block_cnt, int thread_cnt, const double *r
 
 int ves_fp64_fma_rate(double *flops_per_s, void *stream)
 {
-    t_last_error.clear();
+    begin_call();
     if (!flops_per_s) { set_error("null pointer"); return VES_ERR_ARG; }
     return native(cuda_ok(ves::fp64_fma_rate(flops_per_s, (cudaStream_t)stream), "fp64 probe"));
 }

@@ -225,4 +225,12 @@ cudaError_t launch_transpose(bool to_soa, const double *src_re, const double *sr
     return cudaGetLastError();
 }
 
+void load_extras_kernels()
+{
+    load_kernel(eigvals_fp64_kernel);
+    load_kernel(polyroots_kernel);
+    load_kernel(aos_to_soa_kernel);
+    load_kernel(soa_to_aos_kernel);
+}
+
 }  // namespace ves

@@ -128,4 +128,23 @@ void set_error_message(const char *msg);
 // Measured FP64 FMA throughput of this GPU (2 flops per FMA).
 cudaError_t fp64_fma_rate(double *flops_per_s, cudaStream_t st);
 
+// CUDA loads a kernel lazily, at its first launch, by default, so where a
+// kernel's code lands depends on what the process loaded before.  Kernels that
+// run at the same time on one SM (the FP32+refine form's Schur and refinement
+// stages) measured up to 9% slower when loaded late in a long process than
+// when loaded early.  load_kernels() loads every kernel of the library, in
+// one fixed order, the first time it is called for the current device; each
+// file's list below is in that order.
+void load_kernels();
+void load_mixed_kernels();
+void load_fused_kernels();
+void load_varsize_kernels();
+void load_extras_kernels();
+void load_shiftnet_kernels();
+template <typename K> inline void load_kernel(K *k)
+{
+    cudaFuncAttributes fa;
+    cudaFuncGetAttributes(&fa, k);  // forces the load; errors are cleared by load_kernels()
+}
+
 }  // namespace ves

@@ -571,4 +571,19 @@ cudaError_t fp64_fma_rate(double *flops_per_s, cudaStream_t st)
     return e;
 }
 
+void load_fused_kernels()
+{
+    load_kernel(fused_fp64_kernel<false>);
+    load_kernel(fused_fp64_kernel<true>);
+    load_kernel(polish32_warp_kernel);
+    load_kernel(zgehrd_kernel);
+    load_kernel(zunghr_kernel);
+    load_kernel(hessenberg_kernel);
+    load_kernel(zlahqr_kernel);
+    load_kernel(ztrevc_kernel);
+    load_kernel(zgemv_kernel);
+    load_kernel(backsubs_kernel);
+    load_kernel(fp64_fma_probe_kernel);
+}
+
 }  // namespace ves

@@ -640,4 +640,17 @@ cudaError_t launch_mixed_overlap(const MixedArgs &a0, cudaStream_t st, cudaStrea
     return e;
 }
 
+// The pairs that overlap come first: the lane Schur kernel with its refinement,
+// then the warp Schur kernel with its refinement.
+void load_mixed_kernels()
+{
+    load_kernel(schur32_kernel);
+    load_kernel(refine_kernel<16, false>);
+    load_kernel(refine_kernel<32, false>);
+    load_kernel(refine_kernel<64, false>);
+    load_kernel(schur32_warp_kernel);
+    load_kernel(refine_kernel<32, true>);
+    load_kernel(refine_kernel<16, true>);
+}
+
 }  // namespace ves

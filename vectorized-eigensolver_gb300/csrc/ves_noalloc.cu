@@ -63,6 +63,7 @@ int ves_eigensolve_noalloc(int dim, int block_cnt, int thread_cnt, const double 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return fail(VES_ERR_CUDA, "ves_eigensolve_noalloc: no usable CUDA device");
+    ves::load_kernels();
     void *scratch = nullptr;
     {
         // Set-up, once per device, on this call's (current) device.

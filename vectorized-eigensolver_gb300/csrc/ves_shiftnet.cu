@@ -419,6 +419,30 @@ __global__ void shifts_out_kernel(long long count, int n, int tc, int nout_pad, 
 inline unsigned nb(long long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
+
+void load_shiftnet_kernels()
+{
+    load_kernel(tc::gemm_bf16_persistent_kernel<64>);
+    load_kernel(tc::gemm_bf16_persistent_kernel<128>);
+    load_kernel(tc::gemm_bf16_persistent_kernel<256>);
+    load_kernel(tc::gemm_bf16_kernel<64>);
+    load_kernel(tc::gemm_bf16_kernel<256>);
+    load_kernel(features_kernel);
+    load_kernel(targets_kernel);
+    load_kernel(colstats_bf16_kernel);
+    load_kernel(target_stats_kernel);
+    load_kernel(chamfer_kernel);
+    load_kernel(gelu_bwd_kernel);
+    load_kernel(dw_kernel<float>);
+    load_kernel(dw_kernel<bf16>);
+    load_kernel(gelu_f32_kernel);
+    load_kernel(dense_out_kernel);
+    load_kernel(dh_kernel);
+    load_kernel(adam_kernel);
+    load_kernel(to_bf16_kernel);
+    load_kernel(shifts_out_kernel);
+}
+
 }  // namespace ves
 
 // ---------------------------------------------------------------------------

@@ -299,4 +299,15 @@ cudaError_t launch_varsize(long long count, int max_dim, const int *dims, const 
     return cudaGetLastError();
 }
 
+void load_varsize_kernels()
+{
+    load_kernel(varsize_solve_kernel);
+    load_kernel(scan_blocks_kernel);
+    load_kernel(scan_sums_kernel);
+    load_kernel(scan_apply_kernel);
+    load_kernel(histogram_kernel);
+    load_kernel(plan_kernel);
+    load_kernel(scatter_kernel);
+}
+
 }  // namespace ves
