@@ -435,22 +435,35 @@ struct SmemCol {  // column of a SmemMat as a vector
     __device__ __forceinline__ void st(int i, cx<float> v) const { p[i - 1] = make_float2(v.r, v.i); }
 };
 
-__device__ __forceinline__ float warp_sum(float v)
+// Sum over a group of G lanes (G = 32: the warp; G = 16: one half of it);
+// mask holds the group's lanes.
+template <int G>
+__device__ __forceinline__ float group_sum(float v, unsigned mask)
 {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
     return v;
 }
+__device__ __forceinline__ float warp_sum(float v) { return group_sum<32>(v, FULL); }
 
-// zgehd2 on the warp's matrix (n <= 32): H = Q^H A Q, the same reflector
-// conventions and per-element operation order as zgehrd_lane; reflector
-// vectors below the subdiagonal, tau(i) in sTau[i - 1].
-__device__ __forceinline__ void hess32_warp(const int n, const SmemMat &H, float2 *sTau, const int lane)
+// The lanes of the G-lane group that lane `lane` of the warp belongs to.
+template <int G>
+__device__ __forceinline__ unsigned group_mask(int lane)
 {
-    const int j = lane + 1;
+    return G == 32 ? FULL : (((1u << G) - 1u) << (lane & ~(G - 1)));
+}
+
+// zgehd2 on a G-lane group's matrix (n <= G): H = Q^H A Q, the same
+// reflector conventions and per-element operation order as zgehrd_lane;
+// reflector vectors below the subdiagonal, tau(i) in sTau[i - 1].  gl is the
+// lane's index in its group, mask the group's lanes.
+template <int G>
+__device__ __forceinline__ void hess_group(const int n, const SmemMat &H, float2 *sTau, const int gl, const unsigned mask)
+{
+    const int j = gl + 1;
     for (int i = 1; i <= n - 1; ++i) {
         const int mm = n - i;
         const cx<float> xk = (j >= i + 2 && j <= n) ? H.ld(j, i) : mk(0.f, 0.f);
-        const float xnorm2 = warp_sum(fmaf(xk.i, xk.i, xk.r * xk.r));
+        const float xnorm2 = group_sum<G>(fmaf(xk.i, xk.i, xk.r * xk.r), mask);
         const cx<float> alpha = H.ld(i + 1, i);
         const bool trivial = (xnorm2 == 0.f) && (alpha.i == 0.f);
         const float beta = trivial ? alpha.r : -copysignf(sqrtf(alpha.r * alpha.r + alpha.i * alpha.i + xnorm2), alpha.r);
@@ -460,10 +473,10 @@ __device__ __forceinline__ void hess32_warp(const int n, const SmemMat &H, float
             t = mk((beta - alpha.r) * rb, -alpha.i * rb);
             scale = cinv(mk(alpha.r - beta, alpha.i));
         }
-        __syncwarp();  // every lane has read alpha and its x element
+        __syncwarp(mask);  // every lane has read alpha and its x element
         if (j >= i + 2 && j <= n) H.st(j, i, cmul(xk, scale));
-        if (lane == 0) sTau[i - 1] = make_float2(t.r, t.i);
-        __syncwarp();
+        if (gl == 0) sTau[i - 1] = make_float2(t.r, t.i);
+        __syncwarp(mask);
         // right: row j of A(1:n, i+1:n) -= tau (A v)_j v^H
         if (j <= n) {
             cx<float> sacc = H.ld(j, i + 1);
@@ -472,7 +485,7 @@ __device__ __forceinline__ void hess32_warp(const int n, const SmemMat &H, float
             H.st(j, i + 1, csub(H.ld(j, i + 1), ts));
             for (int q = 2; q <= mm; ++q) H.st(j, i + q, cnmacc(H.ld(j, i + q), ts, H.ld(i + q, i)));
         }
-        __syncwarp();
+        __syncwarp(mask);
         // left: column j of A(i+1:n, i+1:n) -= conj(tau) v (v^H A)_j
         if (j >= i + 1 && j <= n) {
             const cx<float> tcj = conj(t);
@@ -482,10 +495,15 @@ __device__ __forceinline__ void hess32_warp(const int n, const SmemMat &H, float
             H.st(i + 1, j, csub(H.ld(i + 1, j), ts));
             for (int q = 2; q <= mm; ++q) H.st(i + q, j, cnmac(H.ld(i + q, j), H.ld(i + q, i), ts));
         }
-        __syncwarp();
-        if (lane == 0) H.st(i + 1, i, mk(beta, 0.f));
-        __syncwarp();
+        __syncwarp(mask);
+        if (gl == 0) H.st(i + 1, i, mk(beta, 0.f));
+        __syncwarp(mask);
     }
+}
+
+__device__ __forceinline__ void hess32_warp(const int n, const SmemMat &H, float2 *sTau, const int lane)
+{
+    hess_group<32>(n, H, sTau, lane, FULL);
 }
 
 //

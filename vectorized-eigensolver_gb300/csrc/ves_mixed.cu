@@ -133,42 +133,49 @@ __global__ void __launch_bounds__(kSchurThreads) schur32_kernel(const MixedArgs 
 }
 
 // ---------------------------------------------------------------------------
-// schur32_warp_kernel: the same FP32 Schur stage for n <= 32 with one matrix
-// per warp.  H and Z live in shared memory (column-major, leading dimension
-// n + 1: a row sweep and a column sweep are both free of bank conflicts); lane
-// l owns row l + 1 in column operations and column l + 1 in row operations;
-// the scalar steps (reflectors, shifts, deflation tests) run redundantly on all
-// lanes from shared values, so control flow is uniform and no lane waits for
-// another matrix's sweeps, and H, Z never leave the SM.  Same algorithm and
-// operation order per element as the lane routines (zgehd2, zung2r, zlahqr
-// single shift, ztrevc back substitution); T, Z and the T-eigenvectors X go to
-// the per-matrix buffer layout read by refine_kernel.
+// schur32_warp_kernel<G>: the same FP32 Schur stage with one matrix per group
+// of G lanes: a warp (G = 32, n <= 32) or half a warp (G = 16, n <= 16, two
+// matrices per warp).  H and Z live in shared memory (column-major, leading
+// dimension n + 1: a row sweep and a column sweep are both free of bank
+// conflicts); lane l of a group owns row l + 1 in column operations and
+// column l + 1 in row operations; the scalar steps (reflectors, shifts,
+// deflation tests) run redundantly on all lanes of the group from shared
+// values, so control flow is uniform within a group and H, Z never leave the
+// SM.  The two halves of a warp synchronise only within themselves (group
+// masks on every shuffle, vote and __syncwarp), so each runs its own sweep
+// sequence; where they branch apart the warp runs the two paths in turn.
+// Same algorithm and operation order per element as the lane routines
+// (zgehd2, zung2r, zlahqr single shift, ztrevc back substitution); T, Z and
+// the T-eigenvectors X go to the per-matrix buffer layout read by
+// refine_kernel.
 // ---------------------------------------------------------------------------
-constexpr int kWarpSchurThreads = 128;  // 4 matrices per block
+constexpr int kWarpSchurThreads = 128;  // 4 warps per block
 
 // per-matrix buffer layout: T, Z, X (n*n float2 each, column-major), then a
 // work vector whose first entry holds ||A||_F^2
 __host__ __device__ __forceinline__ long long mat_elems(int n) { return 3LL * n * n + n; }
 
-__host__ __device__ __forceinline__ size_t warp_schur_smem(int n)
+__host__ __device__ __forceinline__ size_t warp_schur_smem(int n, int G)
 {
-    return (size_t)(kWarpSchurThreads / 32) * (2 * n * (n + 1) + n) * sizeof(float2);
+    return (size_t)(kWarpSchurThreads / G) * (2 * n * (n + 1) + n) * sizeof(float2);
 }
 
+template <int G>
 __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const MixedArgs a, float2 *buf, int *flags)
 {
     extern __shared__ float2 wsm[];
     const int n = a.g.n, tc = a.g.tc;
     const long long N = a.g.N;
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gl = threadIdx.x & (G - 1), wib = threadIdx.x / G;  // lane in group, group in block
+    const unsigned gmask = group_mask<G>(threadIdx.x & 31);
     const int lda = n + 1;
     float2 *sH = wsm + (size_t)wib * (2 * n * lda + n);
     float2 *sZ = sH + n * lda, *sTau = sZ + n * lda;
     const SmemMat H{sH, lda}, Z{sZ, lda};
     const long long nn = (long long)n * n;
-    const long long gw = (long long)blockIdx.x * (kWarpSchurThreads / 32) + wib;
-    const long long nw = (long long)gridDim.x * (kWarpSchurThreads / 32);
-    const int j = lane + 1;  // the row / column this lane owns
+    const long long gw = (long long)blockIdx.x * (kWarpSchurThreads / G) + wib;
+    const long long nw = (long long)gridDim.x * (kWarpSchurThreads / G);
+    const int j = gl + 1;  // the row / column this lane owns
     const float ulp = lim<float>::eps();
     const float smlnum = lim<float>::tiny() * ((float)n / ulp);
 
@@ -177,7 +184,7 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
         const long long mo = soa_off_m(m, nn, tc);
         bool bad = false;
         float s2 = 0.f;
-        for (int e = lane; e < nn; e += 32) {
+        for (int e = gl; e < nn; e += G) {
             const long long k = mo + (long long)e * tc;
             const double re = a.rA[k], im = a.iA[k];
             bad |= nonfinite(re) | nonfinite(im);
@@ -185,12 +192,12 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
             s2 = fmaf(fi, fi, fmaf(fr, fr, s2));
             sH[(e % n) + (e / n) * lda] = make_float2(fr, fi);
         }
-        const float nA2 = warp_sum(s2);
-        bool fb = __any_sync(FULL, bad) || !(nA2 < 1e36f);
+        const float nA2 = group_sum<G>(s2, gmask);
+        bool fb = __any_sync(gmask, bad) || !(nA2 < 1e36f);
         int status = 0, sweeps = 0;
-        __syncwarp();
+        __syncwarp(gmask);
         if (!fb) {
-            hess32_warp(n, H, sTau, lane);
+            hess_group<G>(n, H, sTau, gl, gmask);
             // ---- zung2r: Z = Q from the reflectors, last reflector first
             for (int i = n - 1; i >= 1; --i) {
                 const cx<float> t = mk(sTau[i - 1].x, sTau[i - 1].y);
@@ -202,11 +209,11 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
                     Z.st(c, j, csub(Z.ld(c, j), ts));
                     for (int k = c + 1; k <= n; ++k) Z.st(k, j, cnmac(Z.ld(k, j), H.ld(k, i), ts));
                 }
-                __syncwarp();
+                __syncwarp(gmask);
                 if (j >= c + 1 && j <= n) Z.st(j, c, cmul(H.ld(j, i), mk(-t.r, -t.i)));
                 if (j == c) Z.st(c, c, mk(1.f - t.r, -t.i));
                 if (j >= 2 && j <= c - 1) Z.st(j, c, mk(0.f, 0.f));
-                __syncwarp();
+                __syncwarp(gmask);
             }
             if (j <= n) {
                 Z.st(j, 1, mk(j == 1 ? 1.f : 0.f, 0.f));
@@ -215,31 +222,31 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
             // clear below the subdiagonal: column j, rows j+2..n
             if (j <= n)
                 for (int k = j + 2; k <= n; ++k) H.st(k, j, mk(0.f, 0.f));
-            __syncwarp();
+            __syncwarp(gmask);
             // ---- make the subdiagonal real
             for (int i = 2; i <= n; ++i) {
                 const cx<float> h = H.ld(i, i - 1);
                 if (h.i != 0.f) {
                     cx<float> sc = cscal(h, 1.f / cabs1(h));
                     sc = cscal(conj(sc), 1.f / cabs(sc));
-                    __syncwarp();
-                    if (lane == 0) H.st(i, i - 1, mk(cabs(h), 0.f));
+                    __syncwarp(gmask);
+                    if (gl == 0) H.st(i, i - 1, mk(cabs(h), 0.f));
                     if (j >= i && j <= n) H.st(i, j, cmul(H.ld(i, j), sc));
-                    __syncwarp();
+                    __syncwarp(gmask);
                     const int re = (i + 1) < n ? (i + 1) : n;
                     if (j <= re) H.st(j, i, cmulc(H.ld(j, i), sc));
                     if (j <= n) Z.st(j, i, cmulc(Z.ld(j, i), sc));
                 }
-                __syncwarp();
+                __syncwarp(gmask);
             }
             // ---- single-shift QR, one matrix, uniform control flow
             int I = n, L = 1, its = 0;
             while (I > 1) {
                 if (its > a.max_its) { status |= ST_ITCAP; --I; L = 1; its = 0; continue; }
                 L = deflation_scan<float>(I, L, H, n, ulp, smlnum);
-                __syncwarp();
-                if (L > 1 && lane == 0) H.st(L, L - 1, mk(0.f, 0.f));
-                __syncwarp();
+                __syncwarp(gmask);
+                if (L > 1 && gl == 0) H.st(L, L - 1, mk(0.f, 0.f));
+                __syncwarp(gmask);
                 if (L >= I) { --I; L = 1; its = 0; continue; }
                 const cx<float> t = qr_shift<float>(I, L, its, H);
                 const cx<float> h11s = csub(H.ld(L, L), t);
@@ -252,8 +259,8 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
                     cx<float> a0 = v0, a1 = v1, t1;
                     if (K > L) { a0 = H.ld(K, K - 1); a1 = H.ld(K + 1, K - 1); }
                     zlarfg2<float>(a0, a1, t1);
-                    __syncwarp();
-                    if (K > L && lane == 0) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(0.f, 0.f)); }
+                    __syncwarp(gmask);
+                    if (K > L && gl == 0) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(0.f, 0.f)); }
                     const cx<float> w1 = a1, cw = conj(w1), c1 = conj(t1);
                     const float t2 = t1.r * w1.r - t1.i * w1.i;
                     if (j >= K && j <= n) {  // rows K, K+1, column j
@@ -262,7 +269,7 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
                         H.st(K, j, h1);
                         H.st(K + 1, j, h2);
                     }
-                    __syncwarp();
+                    __syncwarp(gmask);
                     const int je = (K + 2) < I ? (K + 2) : I;
                     if (j <= je) {  // columns K, K+1, row j
                         cx<float> h1 = H.ld(j, K), h2 = H.ld(j, K + 1);
@@ -276,32 +283,32 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
                         Z.st(j, K, z1);
                         Z.st(j, K + 1, z2);
                     }
-                    __syncwarp();
+                    __syncwarp(gmask);
                 }
                 // make H(I, I-1) real
                 const cx<float> h = H.ld(I, I - 1);
                 if (h.i != 0.f) {
                     const float d = cabs(h);
                     const cx<float> z = conj(cscal(h, 1.f / d));
-                    __syncwarp();
-                    if (lane == 0) H.st(I, I - 1, mk(d, 0.f));
+                    __syncwarp(gmask);
+                    if (gl == 0) H.st(I, I - 1, mk(d, 0.f));
                     if (j >= I + 1 && j <= n) H.st(I, j, cmul(H.ld(I, j), z));
                     if (j <= I - 1) H.st(j, I, cmulc(H.ld(j, I), z));
                     if (j <= n) Z.st(j, I, cmulc(Z.ld(j, I), z));
                 }
-                __syncwarp();
+                __syncwarp(gmask);
             }
             if (status & ST_ITCAP) fb = true;
         }
         float2 *out = buf + m * mat_elems(n);
         if (!fb) {
             // T (upper triangle) and Z to the buffer, coalesced
-            for (int e = lane; e < nn; e += 32) {
+            for (int e = gl; e < nn; e += G) {
                 const int r = e % n, c = e / n;
                 out[e] = r <= c ? sH[r + c * lda] : make_float2(0.f, 0.f);
                 out[nn + e] = sZ[r + c * lda];
             }
-            __syncwarp();
+            __syncwarp(gmask);
             // T-eigenvectors: lane j solves column j into sZ (Z is saved)
             if (j <= n) {
                 const SmemCol xc{sZ + (j - 1) * lda};
@@ -311,17 +318,17 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
                 xc.st(j, mk(sc, 0.f));
                 for (int i = j + 1; i <= n; ++i) xc.st(i, mk(0.f, 0.f));
             }
-            __syncwarp();
-            for (int e = lane; e < nn; e += 32) out[2 * nn + e] = sZ[(e % n) + (e / n) * lda];
+            __syncwarp(gmask);
+            for (int e = gl; e < nn; e += G) out[2 * nn + e] = sZ[(e % n) + (e / n) * lda];
         }
-        if (lane == 0) {
+        if (gl == 0) {
             out[3 * nn] = make_float2(nA2, 0.f);  // ||A||_F^2 for the refinement's tolerance
             flags[m] = fb ? 1 : 0;
             if (fb) to_fp64_list(a, flags, m);
             if (a.status) a.status[m] = status;
             if (a.sweeps) a.sweeps[m] = sweeps;
         }
-        __syncwarp();
+        __syncwarp(gmask);
     }
 }
 
@@ -481,35 +488,43 @@ size_t mixed_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blo
 
 namespace {
 
-// Which FP32 Schur kernel: the warp-per-matrix one for 24 <= n <= 32 (measured
-// on GB300, FP32+refine eigensolves/s lane -> warp: n=16 5.34 -> 4.26 M/s,
-// n=24 1.59 -> 1.63 M/s, n=32 0.66 -> 0.72 M/s: below 24 too many lanes idle
-// and the serial reflector steps dominate), the lane-per-matrix one otherwise.  VES_MIXED_SCHUR=lane|warp overrides (for tests and tuning;
-// warp only applies to n <= 32).
-bool use_warp_schur(int n)
+// Which FP32 Schur kernel: 0 = schur32_kernel (a matrix per lane), G = 16 or
+// 32 = schur32_warp_kernel<G> (a matrix per G lanes).  Measured on GB300,
+// FP32+refine eigensolves/s, lane -> warp (G = 32): n=16 5.34 -> 4.26 M/s,
+// n=24 1.59 -> 1.63 M/s, n=32 0.66 -> 0.72 M/s (below 24 too many lanes of a
+// warp idle).  Two matrices per warp (G = 16) does not recover it: with the
+// Schur and refinement stages overlapped, lane -> G = 16 measured n=8 39.9 ->
+// 21.0, n=12 14.1 -> 9.3, n=16 5.84 -> 4.75 M/s (its Schur stage alone at
+// n=16: 90 ms per 1,048,576 matrices against about 78 for the lane kernel,
+// and it leaves less of each SM to the refinement running beside it).
+// Default: G = 32 for 24 <= n <= 32, the lane kernel otherwise.
+// VES_MIXED_SCHUR overrides (tests and tuning): lane; warp (G = 16 for
+// n <= 16, G = 32 for n <= 32); warp16; warp32.
+int schur_group(int n)
 {
-    int mode = 0;  // 0 auto, 1 lane, 2 warp; read per launch (a getenv is cheap next to a solve)
-    if (const char *e = getenv("VES_MIXED_SCHUR")) {
-        if (!strcmp(e, "lane")) mode = 1;
-        if (!strcmp(e, "warp")) mode = 2;
-    }
-    if (n > 32 || mode == 1) return false;
-    return mode == 2 || n >= 24;
+    const char *e = getenv("VES_MIXED_SCHUR");  // read per launch: a getenv is cheap next to a solve
+    if (e && !strcmp(e, "lane")) return 0;
+    if (e && !strcmp(e, "warp")) return n <= 16 ? 16 : (n <= 32 ? 32 : 0);
+    if (e && !strcmp(e, "warp16")) return n <= 16 ? 16 : 0;
+    if (e && !strcmp(e, "warp32")) return n <= 32 ? 32 : 0;
+    return (n >= 24 && n <= 32) ? 32 : 0;
 }
 
+template <int G>
 long long warp_schur_blocks(int n, long long N, int blocks_per_sm)
 {
     // per call (per device, thread safe; microseconds next to the kernel)
-    cudaFuncSetAttribute(schur32_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warp_schur_smem(32));
+    cudaFuncSetAttribute(schur32_warp_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)warp_schur_smem(G, G));
     const int sms = device_sms();
     int per_sm = blocks_per_sm;
     if (per_sm <= 0) {
         per_sm = 1;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, schur32_warp_kernel, kWarpSchurThreads,
-                                                      warp_schur_smem(n));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, schur32_warp_kernel<G>, kWarpSchurThreads,
+                                                      warp_schur_smem(n, G));
         if (per_sm < 1) per_sm = 1;
     }
-    const long long need = (N + kWarpSchurThreads / 32 - 1) / (kWarpSchurThreads / 32);
+    const long long need = (N + kWarpSchurThreads / G - 1) / (kWarpSchurThreads / G);
     return std::max<long long>(1, std::min<long long>(need, (long long)sms * per_sm));
 }
 
@@ -536,9 +551,13 @@ cudaError_t launch_schur(const MixedArgs &a, int blocks_per_sm, cudaStream_t st)
     const int n = a.g.n;
     const long long cnt = a.m_end - a.m_begin;
     const MixedBufs b = mixed_bufs(a);
-    if (use_warp_schur(n))
-        schur32_warp_kernel<<<(unsigned)warp_schur_blocks(n, cnt, blocks_per_sm), kWarpSchurThreads,
-                              warp_schur_smem(n), st>>>(a, b.buf, b.flags);
+    const int G = schur_group(n);
+    if (G == 16)
+        schur32_warp_kernel<16><<<(unsigned)warp_schur_blocks<16>(n, cnt, blocks_per_sm), kWarpSchurThreads,
+                                  warp_schur_smem(n, 16), st>>>(a, b.buf, b.flags);
+    else if (G == 32)
+        schur32_warp_kernel<32><<<(unsigned)warp_schur_blocks<32>(n, cnt, blocks_per_sm), kWarpSchurThreads,
+                                  warp_schur_smem(n, 32), st>>>(a, b.buf, b.flags);
     else
         schur32_kernel<<<(unsigned)schur_blocks(cnt, blocks_per_sm), kSchurThreads, 0, st>>>(a, b.buf, b.flags);
     return cudaGetLastError();
@@ -551,7 +570,7 @@ cudaError_t launch_refine(const MixedArgs &a, cudaStream_t st)
     const MixedBufs b = mixed_bufs(a);
     const long long pairs = (a.m_end - a.m_begin) * n;
     const unsigned rb = (unsigned)((pairs + kRefineThreads - 1) / kRefineThreads);
-    if (use_warp_schur(n)) {
+    if (schur_group(n)) {  // per-matrix buffer layout
         if (n <= 16)
             refine_kernel<16, true><<<rb, kRefineThreads, 0, st>>>(a, b.buf, b.flags);
         else
@@ -605,7 +624,7 @@ cudaError_t launch_mixed_overlap(const MixedArgs &a0, cudaStream_t st, cudaStrea
     // FP32+refine eigensolves/s serial -> overlapped: n=8 36.1 -> 41.0 M/s,
     // n=16 5.10 -> 5.87 M/s, n=24 1.63 -> 1.72 M/s, n=32 0.726 -> 0.846 M/s);
     // VES_MIXED_OVERLAP_BLOCKS_PER_SM overrides
-    int bps = a.blocks_per_sm > 0 ? a.blocks_per_sm : (use_warp_schur(a.g.n) ? 6 : 4);
+    int bps = a.blocks_per_sm > 0 ? a.blocks_per_sm : (schur_group(a.g.n) ? 6 : 4);
     if (a.blocks_per_sm <= 0)
         if (const char *ev = getenv("VES_MIXED_OVERLAP_BLOCKS_PER_SM")) {
             const int v = atoi(ev);
@@ -648,8 +667,9 @@ void load_mixed_kernels()
     load_kernel(refine_kernel<16, false>);
     load_kernel(refine_kernel<32, false>);
     load_kernel(refine_kernel<64, false>);
-    load_kernel(schur32_warp_kernel);
+    load_kernel(schur32_warp_kernel<32>);
     load_kernel(refine_kernel<32, true>);
+    load_kernel(schur32_warp_kernel<16>);
     load_kernel(refine_kernel<16, true>);
 }
 
