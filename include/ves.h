@@ -120,8 +120,9 @@ typedef struct ves_options {
     int precision;     /* VES_PREC_*; default FP64 */
     int max_its;       /* sweeps per eigenvalue = max_its + 1; default 30 (reference Toolbox.hpp:808) */
     int vnorm;         /* eigenvector scaling, VES_VNORM_*; default REFERENCE */
-    int refine_steps;  /* FP32_REFINE: Newton corrections per eigenpair before falling back to FP64; default 3 */
-    double refine_tol; /* FP32_REFINE: accept when ||A v - lambda v|| <= refine_tol ||A||_F ||v||; default 5e-14 */
+    int refine_steps;  /* FP32_REFINE: Newton corrections per eigenpair before falling back to FP64; default 8 */
+    double refine_tol; /* FP32_REFINE: accept when ||A v - lambda v|| <= refine_tol ||A||_F ||v|| and the
+                        * correction that residual gives to lambda is <= 4 refine_tol ||A||_F; default 5e-14 */
     int want_vectors;  /* 1 (default): eigenvalues and eigenvectors; 0: eigenvalues only (FP64; the QR
                         * runs on the active block only, no Q and no Schur vectors -- the same
                         * eigenvalues, about a third of the QR work; rV/iV may be NULL) */
@@ -146,9 +147,11 @@ size_t ves_eigensolve_workspace_size(int dim, int block_cnt, int thread_cnt, con
  * precision = VES_PREC_FP64: the reference path in FP64 (one launch).
  * precision = VES_PREC_FP32_REFINE: the reference path in complex FP32, then
  *   every eigenpair refined by Newton steps whose residual is computed in
- *   FP64, until ||A v - lambda v|| <= refine_tol ||A||_F ||v||; a matrix that
- *   does not get there (or whose FP32 QR hit the sweep cap, or whose data do
- *   not fit FP32) is solved again in FP64 (status bit VES_STATUS_REFINE_FALLBACK).
+ *   FP64, until ||A v - lambda v|| <= refine_tol ||A||_F ||v|| and the next
+ *   Newton correction to lambda (its error estimate) is <= 4 refine_tol
+ *   ||A||_F; a matrix that does not get there within refine_steps corrections
+ *   (or whose FP32 QR hit the sweep cap, or whose data do not fit FP32) is
+ *   solved again in FP64 (status bit VES_STATUS_REFINE_FALLBACK).
  *   Eigenvalues come in the FP32 Schur order; the REFERENCE eigenvector scaling
  *   (unit component along the k-th Schur vector) then holds to FP32 accuracy.
  *   rT/iT must be NULL in this mode.

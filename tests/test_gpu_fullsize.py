@@ -193,3 +193,41 @@ def test_fullsize_learned_config():
     Ah = ves.complex_from_soa(rA[:k].cpu().numpy(), iA[:k].cpu().numpy(), n, TC)
     _, err, _ = match_eigs(Eg, Eo)
     assert (err / np.linalg.norm(Ah, axis=(1, 2))).max() <= 1e-12
+
+
+@pytest.mark.parametrize("name", ["gauss16", "gauss32"])
+def test_fullsize_fp32_refine_eigenvalues(name):
+    """FP32 + refinement over the whole batch: every eigenvalue within
+    1e-12 ||A||_F of the plain FP64 solve's nearest one and every residual
+    <= 1e-13.  (Accepting a pair on its residual alone let an eigenvalue with
+    condition number ~50 land 2.3e-12 ||A||_F away on this batch; the
+    refinement also checks the size of its next correction to lambda.)"""
+    import torch
+    w = workloads.WORKLOADS[name]
+    N, n, seed = w["N"], w["n"], w["seed"]
+    bc = N // TC
+    rA, iA = workloads.gaussian_soa(N, n, seed, TC)
+    dA = [torch.from_numpy(rA).cuda(), torch.from_numpy(iA).cuda()]
+    del rA, iA
+    outs = []
+    for prec in (ves.VES_PREC_FP64, ves.VES_PREC_FP32_REFINE):
+        dE = [torch.empty(N * n, dtype=torch.float64, device="cuda") for _ in range(2)]
+        dV = [torch.empty_like(dA[0]) for _ in range(2)]
+        st = torch.full((N,), -1, dtype=torch.int32, device="cuda")
+        ves.eigensolve(n, bc, TC, dA[0], dA[1], dE[0], dE[1], dV[0], dV[1], status=st,
+                       options=ves.default_options(precision=prec))
+        torch.cuda.synchronize()
+        outs.append((dE, dV, st))
+    st = outs[1][2]
+    assert int(((st & ~ves.VES_STATUS_REFINE_FALLBACK) != 0).sum()) == 0
+    assert int(((st & ves.VES_STATUS_REFINE_FALLBACK) != 0).sum()) <= N // 100_000
+    A = soa_planes_to_batch(dA[0], dA[1], n, TC)
+    E64 = soa_vec_to_batch(outs[0][0][0], outs[0][0][1], n, TC)
+    E = soa_vec_to_batch(outs[1][0][0], outs[1][0][1], n, TC)
+    V = soa_planes_to_batch(outs[1][1][0], outs[1][1][1], n, TC)
+    assert float(device_residuals(A, E, V).max()) <= 1e-13
+    worst = 0.0
+    for s in range(0, N, 1 << 16):
+        d = (E[s:s + (1 << 16), :, None] - E64[s:s + (1 << 16), None, :]).abs().amin(dim=2)
+        worst = max(worst, float((d / torch.linalg.matrix_norm(A[s:s + (1 << 16)])[:, None]).max()))
+    assert worst <= 1e-12, worst

@@ -537,7 +537,7 @@ void ves_default_options(ves_options *opt)
     opt->precision = VES_PREC_FP64;
     opt->max_its = 30;
     opt->vnorm = VES_VNORM_REFERENCE;
-    opt->refine_steps = 3;
+    opt->refine_steps = 8;
     opt->refine_tol = 5e-14;
     opt->want_vectors = 1;
     opt->blocks_per_sm = 0;
