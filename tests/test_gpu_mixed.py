@@ -45,15 +45,23 @@ def test_mixed_matches_oracle(n, N, tc):
     assert (out["status"] & ~ves.VES_STATUS_REFINE_FALLBACK == 0).all()
 
 
-def test_mixed_forced_fallback_equals_fp64():
+@pytest.mark.parametrize("n,N,tc,vnorm", [(10, 96, 32, 0), (1, 64, 32, 0), (2, 96, 8, 0), (5, 160, 32, 1),
+                                         (16, 96, 32, 2), (24, 64, 16, 0), (32, 96, 32, 1), (40, 64, 32, 0),
+                                         (16, 5000, 40, 0), (32, 5120, 512, 2)])
+def test_mixed_forced_fallback_equals_fp64(n, N, tc, vnorm):
     """With no Newton step allowed nothing can be certified: every matrix goes
-    through the FP64 solver and the result is the FP64 result bit for bit."""
-    rng = np.random.default_rng(3)
-    A = cgauss(rng, (96, 10, 10))
-    fp64 = run_fused(A, 32)
-    import torch  # noqa: F401
-    out = run_fused_opts(A, 32, precision=MIX, refine_steps=0)
+    through the FP64 solver and the result is the plain FP64 result bit for
+    bit, sweep counts included.  For n <= 32 the first list entries (one per
+    warp slot of the GPU) go to the warp-per-matrix FP64 kernel and the rest
+    (N = 5000, 5120) to the lane kernel; n = 40 is the lane kernel only."""
+    rng = np.random.default_rng(3 + n)
+    A = cgauss(rng, (N, n, n))
+    A[3] = np.triu(A[3])  # already triangular: the reflectors' trivial branch
+    fp64 = run_fused_opts(A, tc, vnorm=vnorm)
+    out = run_fused_opts(A, tc, precision=MIX, refine_steps=0, vnorm=vnorm)
     assert ((out["status"] & ves.VES_STATUS_REFINE_FALLBACK) != 0).all()
+    np.testing.assert_array_equal(out["status"] & ~ves.VES_STATUS_REFINE_FALLBACK, fp64["status"])
+    np.testing.assert_array_equal(out["sweeps"], fp64["sweeps"])
     np.testing.assert_array_equal(out["E"], fp64["E"])
     np.testing.assert_array_equal(out["V"], fp64["V"])
 
@@ -68,10 +76,12 @@ def run_fused_opts(A, tc, **kw):
     dEr = torch.empty(N * n, dtype=torch.float64, device="cuda"); dEi = torch.empty_like(dEr)
     dVr, dVi = torch.empty_like(dAr), torch.empty_like(dAi)
     st = torch.full((N,), -1, dtype=torch.int32, device="cuda")
-    ves.eigensolve(n, bc, tc, dAr, dAi, dEr, dEi, dVr, dVi, status=st, options=ves.default_options(**kw))
+    sw = torch.full((N,), -1, dtype=torch.int32, device="cuda")
+    ves.eigensolve(n, bc, tc, dAr, dAi, dEr, dEi, dVr, dVi, status=st, sweeps=sw, options=ves.default_options(**kw))
     torch.cuda.synchronize()
     return dict(E=ves.complex_vec_from_soa(dEr.cpu().numpy(), dEi.cpu().numpy(), n, tc),
-                V=ves.complex_from_soa(dVr.cpu().numpy(), dVi.cpu().numpy(), n, tc), status=st.cpu().numpy())
+                V=ves.complex_from_soa(dVr.cpu().numpy(), dVi.cpu().numpy(), n, tc), status=st.cpu().numpy(),
+                sweeps=sw.cpu().numpy())
 
 
 def test_mixed_nonfinite_and_degenerate():

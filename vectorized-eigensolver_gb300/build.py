@@ -22,6 +22,7 @@ OBJDIR = os.path.join(HERE, "_build")
 SOURCES = ["ves_kernels.cu", "ves_mixed.cu", "ves_extras.cu", "ves_varsize.cu", "ves_noalloc.cu", "ves_shiftnet.cu", "ves_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
+EXTRA = {}  # per-source extra nvcc flags
 
 
 def _nvcc():
@@ -45,7 +46,7 @@ def build(force=False, verbose=False):
 
     def compile_one(src):
         obj = os.path.join(OBJDIR, os.path.splitext(src)[0] + ".o")
-        cmd = [nvcc] + ARCH + FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc] + ARCH + FLAGS + EXTRA.get(src, []) + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr))

@@ -662,7 +662,7 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
     if (!cuda_ok(me, "mixed-precision kernel launch")) return VES_ERR_CUDA;
     a.list = list;
     a.list_count = count;
-    return native(cuda_ok(ves::launch_fused_fp64(a, st), "fallback kernel launch"));
+    return native(cuda_ok(ves::launch_fp64_list(a, st), "fallback kernel launch"));
 }
 
 size_t ves_polyroots_workspace_size(int degree, int block_cnt, int thread_cnt)

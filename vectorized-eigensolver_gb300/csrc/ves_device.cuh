@@ -34,12 +34,17 @@ template <class R> struct cx { R r, i; };
 
 template <class R> __device__ __forceinline__ cx<R> mk(R r, R i) { cx<R> z; z.r = r; z.i = i; return z; }
 template <class R> __device__ __forceinline__ R cabs1(cx<R> z) { return fabs(z.r) + fabs(z.i); }
-template <class R> __device__ __forceinline__ R cabs(cx<R> z) { return sqrt(z.r * z.r + z.i * z.i); }
-template <class R> __device__ __forceinline__ cx<R> cmul(cx<R> a, cx<R> b) { return mk(a.r * b.r - a.i * b.i, a.i * b.r + a.r * b.i); }
+// Products and sums of products are written with explicit fma(): what the
+// compiler would fuse on its own depends on the code around an inlined
+// helper, so the same expression could round differently in two kernels.
+// Written out, every kernel that inlines a helper computes the same bits
+// (the lane, warp-per-matrix and eigenvalues-only FP64 solvers rely on it).
+template <class R> __device__ __forceinline__ R cabs(cx<R> z) { return sqrt(fma(z.r, z.r, z.i * z.i)); }
+template <class R> __device__ __forceinline__ cx<R> cmul(cx<R> a, cx<R> b) { return mk(fma(a.r, b.r, -(a.i * b.i)), fma(a.i, b.r, a.r * b.i)); }
 // a * conj(b)
-template <class R> __device__ __forceinline__ cx<R> cmulc(cx<R> a, cx<R> b) { return mk(a.r * b.r + a.i * b.i, a.i * b.r - a.r * b.i); }
+template <class R> __device__ __forceinline__ cx<R> cmulc(cx<R> a, cx<R> b) { return mk(fma(a.r, b.r, a.i * b.i), fma(a.i, b.r, -(a.r * b.i))); }
 // conj(a) * b
-template <class R> __device__ __forceinline__ cx<R> cjmul(cx<R> a, cx<R> b) { return mk(a.r * b.r + a.i * b.i, a.r * b.i - a.i * b.r); }
+template <class R> __device__ __forceinline__ cx<R> cjmul(cx<R> a, cx<R> b) { return mk(fma(a.r, b.r, a.i * b.i), fma(a.r, b.i, -(a.i * b.r))); }
 template <class R> __device__ __forceinline__ cx<R> cadd(cx<R> a, cx<R> b) { return mk(a.r + b.r, a.i + b.i); }
 template <class R> __device__ __forceinline__ cx<R> csub(cx<R> a, cx<R> b) { return mk(a.r - b.r, a.i - b.i); }
 template <class R> __device__ __forceinline__ cx<R> cscal(cx<R> a, R d) { return mk(a.r * d, a.i * d); }
@@ -85,11 +90,11 @@ template <class R> __device__ __forceinline__ cx<R> cinv(cx<R> z)
 {
     if (fabs(z.r) <= fabs(z.i)) {
         R ratio = z.r / z.i;
-        R rden = R(1) / (z.i * (R(1) + ratio * ratio));
+        R rden = R(1) / (z.i * fma(ratio, ratio, R(1)));
         return mk(ratio * rden, -rden);
     } else {
         R ratio = z.i / z.r;
-        R rden = R(1) / (z.r * (R(1) + ratio * ratio));
+        R rden = R(1) / (z.r * fma(ratio, ratio, R(1)));
         return mk(rden, -ratio * rden);
     }
 }
@@ -97,12 +102,12 @@ template <class R> __device__ __forceinline__ cx<R> cdiv(cx<R> a, cx<R> b)
 {
     if (fabs(b.r) <= fabs(b.i)) {
         R ratio = b.r / b.i;
-        R rden = R(1) / (b.i * (R(1) + ratio * ratio));
-        return mk((a.r * ratio + a.i) * rden, (a.i * ratio - a.r) * rden);
+        R rden = R(1) / (b.i * fma(ratio, ratio, R(1)));
+        return mk(fma(a.r, ratio, a.i) * rden, fma(a.i, ratio, -a.r) * rden);
     } else {
         R ratio = b.i / b.r;
-        R rden = R(1) / (b.r * (R(1) + ratio * ratio));
-        return mk((a.r + a.i * ratio) * rden, (a.i - a.r * ratio) * rden);
+        R rden = R(1) / (b.r * fma(ratio, ratio, R(1)));
+        return mk(fma(a.i, ratio, a.r) * rden, fma(-a.r, ratio, a.i) * rden);
     }
 }
 // principal square root (ComplexDouble.hpp:451-488 semantics)
@@ -207,7 +212,7 @@ __device__ void zgehrd_lane(const int n, const M &A, const V &tau)
             xnorm2 = fma(x.i, x.i, fma(x.r, x.r, xnorm2));
         }
         const bool trivial = (xnorm2 == R(0)) && (alpha.i == R(0));
-        const R beta = trivial ? alpha.r : -copysign(sqrt(alpha.r * alpha.r + alpha.i * alpha.i + xnorm2), alpha.r);
+        const R beta = trivial ? alpha.r : -copysign(sqrt(fma(alpha.r, alpha.r, fma(alpha.i, alpha.i, xnorm2))), alpha.r);
         cx<R> t = mk(R(0), R(0));
         cx<R> scale = mk(R(0), R(0));
         if (!trivial) {
@@ -360,8 +365,8 @@ __device__ __forceinline__ int deflation_scan(const int I, const int L0, const M
 template <class R, class MH>
 __device__ __forceinline__ cx<R> qr_shift(const int I, const int L, const int its, const MH &H)
 {
-    if (its == 10) return cadd(mk(R(0.75) * fabs(H.ld(L + 1, L).r), R(0)), H.ld(L, L));
-    if (its == 20) return cadd(mk(R(0.75) * fabs(H.ld(I, I - 1).r), R(0)), H.ld(I, I));
+    if (its == 10) { const cx<R> h = H.ld(L, L); return mk(fma(R(0.75), fabs(H.ld(L + 1, L).r), h.r), h.i); }
+    if (its == 20) { const cx<R> h = H.ld(I, I); return mk(fma(R(0.75), fabs(H.ld(I, I - 1).r), h.r), h.i); }
     cx<R> t = H.ld(I, I);
     const cx<R> u = cmul(csqrt(H.ld(I - 1, I)), csqrt(H.ld(I, I - 1)));
     R s = cabs1(u);
@@ -374,7 +379,7 @@ __device__ __forceinline__ cx<R> qr_shift(const int I, const int L, const int it
         cx<R> y = cscal(csqrt(cadd(cmul(xs, xs), cmul(us, us))), s);
         if (sx > R(0)) {
             const R rsx = R(1) / sx;
-            if ((x.r * rsx) * y.r + (x.i * rsx) * y.i < R(0)) y = mk(-y.r, -y.i);
+            if (fma(x.r * rsx, y.r, (x.i * rsx) * y.i) < R(0)) y = mk(-y.r, -y.i);
         }
         t = csub(t, cmul(cdiv(u, cadd(x, y)), u));
     }
@@ -392,7 +397,7 @@ __device__ __forceinline__ void zlarfg2(cx<R> &v0, cx<R> &v1, cx<R> &t1)
         return;
     }
     const R safmin = lim<R>::tiny() / (lim<R>::eps() * R(0.5));
-    R norm = sqrt(v0.r * v0.r + v0.i * v0.i + v1.r * v1.r + v1.i * v1.i);
+    R norm = sqrt(fma(v1.i, v1.i, fma(v1.r, v1.r, fma(v0.i, v0.i, v0.r * v0.r))));
     int knt = 0;
     if (norm < safmin) {
         const R rs = R(1) / safmin;
@@ -402,7 +407,7 @@ __device__ __forceinline__ void zlarfg2(cx<R> &v0, cx<R> &v1, cx<R> &t1)
             v0 = cscal(v0, rs);
             norm *= rs;
         } while (norm < safmin && knt < 40);
-        norm = sqrt(v0.r * v0.r + v0.i * v0.i + v1.r * v1.r + v1.i * v1.i);
+        norm = sqrt(fma(v1.i, v1.i, fma(v1.r, v1.r, fma(v0.i, v0.i, v0.r * v0.r))));
     }
     R beta = copysign(norm, v0.r);
     const cx<R> z = mk(v0.r + beta, v0.i);
@@ -466,7 +471,7 @@ __device__ __forceinline__ void hess_group(const int n, const SmemMat &H, float2
         const float xnorm2 = group_sum<G>(fmaf(xk.i, xk.i, xk.r * xk.r), mask);
         const cx<float> alpha = H.ld(i + 1, i);
         const bool trivial = (xnorm2 == 0.f) && (alpha.i == 0.f);
-        const float beta = trivial ? alpha.r : -copysignf(sqrtf(alpha.r * alpha.r + alpha.i * alpha.i + xnorm2), alpha.r);
+        const float beta = trivial ? alpha.r : -copysignf(sqrtf(fmaf(alpha.r, alpha.r, fmaf(alpha.i, alpha.i, xnorm2))), alpha.r);
         cx<float> t = mk(0.f, 0.f), scale = mk(0.f, 0.f);
         if (!trivial) {
             const float rb = 1.f / beta;
@@ -691,7 +696,7 @@ __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool va
                 if (K > L) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(R(0), R(0))); }
                 w1 = a1;
             }
-            const R t2 = t1.r * w1.r - t1.i * w1.i;
+            const R t2 = fma(t1.r, w1.r, -(t1.i * w1.i));
             if (kSchur) {
                 if (act) {
                     // rows K, K+1 of H (columns K..n; wantT: I2 = n) and columns

@@ -28,9 +28,12 @@ struct FusedArgs {
     int max_its;
     int vnorm;
     // optional index list: solve only matrices list[0 .. *list_count) (the
-    // mixed-precision form's fallback pass); status gets ST_REFINE_FALLBACK
+    // mixed-precision form's fallback pass); status gets ST_REFINE_FALLBACK.
+    // The lane kernel takes entries from list_split on, fp64_warp_kernel the
+    // ones before it (launch_fp64_list sets it).
     const int *list;
     const int *list_count;
+    long long list_split;
     // optional predicted eigenvalues (SoA vectors, n per matrix) used as the
     // first `shift_sweeps` QR shifts of every eigenvalue; `fallbacks` (nullable)
     // counts per matrix the eigenvalues that still needed Wilkinson's shift
@@ -77,6 +80,10 @@ cudaError_t launch_mixed_overlap(const MixedArgs &a, cudaStream_t st, cudaStream
 size_t fused_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blocks, int *out_threads,
                              bool learned = false);
 cudaError_t launch_fused_fp64(const FusedArgs &a, cudaStream_t st);
+// The FP64 solve of the matrices on a.list: the first entries (one per warp
+// slot of the GPU) by fp64_warp_kernel (one matrix per warp, n <= 32), the
+// rest by the lane kernel; the same results bit for bit either way.
+cudaError_t launch_fp64_list(FusedArgs a, cudaStream_t st);
 
 // Stage kernels, in place on the SoA layout (reference call_* semantics).
 cudaError_t launch_zgehrd(Geom g, double *rA, double *iA, double *rtau, double *itau, cudaStream_t st);

@@ -47,19 +47,26 @@ __device__ __forceinline__ long long soa_vec_off(long long m, int n, int tc)
 // has a unit entry at position k), 1 = largest |re|+|im| equal to 1 (LAPACK
 // ztrevc), 2 = unit 2-norm.
 template <class R, class MZ>
+__device__ __forceinline__ R vector_scale(const int n, const MZ &Z, const int j, const int vnorm)
+{
+    R scale = R(1);
+    if (vnorm == 1) {
+        R mx = R(0);
+        for (int i = 1; i <= n; ++i) mx = fmax(mx, cabs1(Z.ld(i, j)));
+        scale = mx > R(0) ? R(1) / mx : R(1);
+    } else if (vnorm == 2) {
+        R s2 = R(0);
+        for (int i = 1; i <= n; ++i) { const cx<R> z = Z.ld(i, j); s2 += fma(z.r, z.r, z.i * z.i); }
+        scale = s2 > R(0) ? R(1) / sqrt(s2) : R(1);
+    }
+    return scale;
+}
+
+template <class R, class MZ>
 __device__ void write_vectors(const int n, const MZ &Z, const MatSoA<R> &V, const int vnorm)
 {
     for (int j = 1; j <= n; ++j) {
-        R scale = R(1);
-        if (vnorm == 1) {
-            R mx = R(0);
-            for (int i = 1; i <= n; ++i) mx = fmax(mx, cabs1(Z.ld(i, j)));
-            scale = mx > R(0) ? R(1) / mx : R(1);
-        } else if (vnorm == 2) {
-            R s2 = R(0);
-            for (int i = 1; i <= n; ++i) { const cx<R> z = Z.ld(i, j); s2 += z.r * z.r + z.i * z.i; }
-            scale = s2 > R(0) ? R(1) / sqrt(s2) : R(1);
-        }
+        const R scale = vector_scale<R>(n, Z, j, vnorm);
         for (int i = 1; i <= n; ++i) V.st(i, j, cscal(Z.ld(i, j), scale));
     }
 }
@@ -72,7 +79,7 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
     const int lane = threadIdx.x & 31;
     const long long slot = (long long)blockIdx.x * (kFusedThreads / 32) + (threadIdx.x >> 5);
     const long long nslots = (long long)gridDim.x * (kFusedThreads / 32);
-    const long long Nw = a.list ? (long long)*a.list_count : N;
+    const long long Nw = a.list ? (long long)*a.list_count - a.list_split : N;
     const long long ngroups = (Nw + 31) / 32;
     const long long per_lane = fused_slot_elems(n, kLearned);  // H, Z, work vector (+ FP32 H, predictions)
 
@@ -84,7 +91,7 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
     for (long long g = slot; g < ngroups; g += nslots) {
         const long long idx = g * 32 + lane;
         const bool valid = idx < Nw;
-        const long long m = valid ? (a.list ? (long long)a.list[idx] : idx) : 0;
+        const long long m = valid ? (a.list ? (long long)a.list[a.list_split + idx] : idx) : 0;
         const long long mo = valid ? soa_mat_off(m, n, tc) : 0;
         const long long vo = valid ? soa_vec_off(m, n, tc) : 0;
         int status = 0, sweeps = 0;
@@ -165,6 +172,250 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
             if (a.status) a.status[m] = status | (a.list ? ST_REFINE_FALLBACK : 0);
             if (a.sweeps) a.sweeps[m] = sweeps;
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// fp64_warp_kernel: the fused kernel's FP64 solve (no learned shifts) for
+// n <= 32 with one matrix per warp, H, Z and the T-eigenvectors X in shared
+// memory; for the few matrices on a device list (those the FP32+refine form
+// hands back to FP64).  The lane kernel solves such a list in one or two
+// lanes of one warp, and an FP64 warp instruction costs the same with one
+// active lane as with 32: 11 ms at n = 16 and 72 ms at n = 32 on GB300 for
+// one or two matrices.  Here lane l owns row l + 1 of a column operation and
+// column l + 1 of a row operation (as in schur32_warp_kernel), and each
+// element goes through the same operations in the same order as in the lane
+// routines (zgehrd_lane, zunghr_lane, clear_below_subdiag_lane,
+// make_subdiag_real_lane, zlahqr_warp, ztrevc_lane, write_vectors), the
+// reflector norms summed sequentially as there: the results are the lane
+// kernel's bit for bit.  Scalar steps run redundantly on every lane from
+// shared values.  One warp per block.
+// ---------------------------------------------------------------------------
+struct SmemMat64 {
+    double2 *p;
+    int lda;
+    __device__ __forceinline__ cx<double> ld(int i, int j) const
+    {
+        const double2 v = p[(i - 1) + (j - 1) * lda];
+        return mk(v.x, v.y);
+    }
+    __device__ __forceinline__ void st(int i, int j, cx<double> v) const { p[(i - 1) + (j - 1) * lda] = make_double2(v.r, v.i); }
+};
+struct SmemCol64 {
+    double2 *p;
+    __device__ __forceinline__ cx<double> ld(int i) const { const double2 v = p[i - 1]; return mk(v.x, v.y); }
+    __device__ __forceinline__ void st(int i, cx<double> v) const { p[i - 1] = make_double2(v.r, v.i); }
+};
+
+// double2 elements of shared memory: H, Z, X (n (n + 1) each), tau, scales
+__host__ __device__ __forceinline__ size_t fp64_warp_smem(int n) { return ((size_t)3 * n * (n + 1) + 2 * n) * sizeof(double2); }
+
+__global__ void __launch_bounds__(32) fp64_warp_kernel(const FusedArgs a)
+{
+    extern __shared__ double2 fsm[];
+    const int n = a.g.n, tc = a.g.tc;
+    const int lane = threadIdx.x, j = lane + 1;  // the row / column this lane owns
+    const int lda = n + 1;
+    const SmemMat64 H{fsm, lda}, Z{fsm + n * lda, lda}, X{fsm + 2 * n * lda, lda};
+    double2 *sTau = fsm + 3 * n * lda, *sS = sTau + n;
+    const double ulp = lim<double>::eps();
+    const double smlnum = lim<double>::tiny() * ((double)n / ulp);
+    const long long count = a.list ? (long long)min(*a.list_count, (int)a.list_split) : a.g.N;
+
+    for (long long w = blockIdx.x; w < count; w += gridDim.x) {
+        const long long m = a.list ? (long long)a.list[w] : w;
+        const long long mo = soa_mat_off(m, n, tc), vo = soa_vec_off(m, n, tc);
+        int status = 0, sweeps = 0;
+        bool bad = false;
+        for (int e = lane; e < n * n; e += 32) {
+            const long long k = mo + (long long)e * tc;
+            const double re = a.rA[k], im = a.iA[k];
+            bad |= nonfinite(re) | nonfinite(im);
+            H.st(e % n + 1, e / n + 1, mk(re, im));
+        }
+        if (__any_sync(FULL, bad)) status |= ST_NONFINITE;
+        __syncwarp();
+
+        // ---- zgehrd (zgehd2): reflector i from column i, applied right then left
+        for (int i = 1; i <= n - 1; ++i) {
+            const int mm = n - i;
+            const cx<double> alpha = H.ld(i + 1, i);
+            double xnorm2 = 0.0;
+            for (int k = i + 2; k <= n; ++k) {
+                const cx<double> x = H.ld(k, i);
+                xnorm2 = fma(x.i, x.i, fma(x.r, x.r, xnorm2));
+            }
+            const bool trivial = (xnorm2 == 0.0) && (alpha.i == 0.0);
+            const double beta = trivial ? alpha.r : -copysign(sqrt(fma(alpha.r, alpha.r, fma(alpha.i, alpha.i, xnorm2))), alpha.r);
+            cx<double> t = mk(0.0, 0.0), scale = mk(0.0, 0.0);
+            if (!trivial) {
+                const double rb = 1.0 / beta;
+                t = mk((beta - alpha.r) * rb, -alpha.i * rb);
+                scale = cinv(mk(alpha.r - beta, alpha.i));
+            }
+            __syncwarp();  // every lane has read column i
+            if (j >= i + 2 && j <= n) H.st(j, i, cmul(H.ld(j, i), scale));
+            if (lane == 0) sTau[i - 1] = make_double2(t.r, t.i);
+            __syncwarp();
+            if (j <= n) {  // right: row j of A(1:n, i+1:n) -= tau (A v)_j v^H
+                cx<double> sacc = H.ld(j, i + 1);
+                for (int q = 2; q <= mm; ++q) sacc = cmac(sacc, H.ld(j, i + q), H.ld(i + q, i));
+                const cx<double> ts = cmul(t, sacc);
+                H.st(j, i + 1, csub(H.ld(j, i + 1), ts));
+                for (int q = 2; q <= mm; ++q) H.st(j, i + q, cnmacc(H.ld(j, i + q), ts, H.ld(i + q, i)));
+            }
+            __syncwarp();
+            if (j >= i + 1 && j <= n) {  // left: column j of A(i+1:n, i+1:n) -= conj(tau) v (v^H A)_j
+                const cx<double> tcj = conj(t);
+                cx<double> sacc = H.ld(i + 1, j);
+                for (int q = 2; q <= mm; ++q) sacc = cjmac(sacc, H.ld(i + q, i), H.ld(i + q, j));
+                const cx<double> ts = cmul(tcj, sacc);
+                H.st(i + 1, j, csub(H.ld(i + 1, j), ts));
+                for (int q = 2; q <= mm; ++q) H.st(i + q, j, cnmac(H.ld(i + q, j), H.ld(i + q, i), ts));
+            }
+            __syncwarp();
+            if (lane == 0) H.st(i + 1, i, mk(beta, 0.0));
+            __syncwarp();
+        }
+        // ---- zunghr (zung2r): Z = Q, last reflector first
+        for (int i = n - 1; i >= 1; --i) {
+            const cx<double> t = mk(sTau[i - 1].x, sTau[i - 1].y);
+            const int c = i + 1;
+            if (j >= c + 1 && j <= n) {
+                cx<double> sacc = Z.ld(c, j);
+                for (int k = c + 1; k <= n; ++k) sacc = cjmac(sacc, H.ld(k, i), Z.ld(k, j));
+                const cx<double> ts = cmul(t, sacc);
+                Z.st(c, j, csub(Z.ld(c, j), ts));
+                for (int k = c + 1; k <= n; ++k) Z.st(k, j, cnmac(Z.ld(k, j), H.ld(k, i), ts));
+            }
+            __syncwarp();
+            const cx<double> mt = mk(-t.r, -t.i);
+            if (j >= c + 1 && j <= n) Z.st(j, c, cmul(H.ld(j, i), mt));
+            if (j == c) Z.st(c, c, mk(1.0 - t.r, -t.i));
+            if (j >= 2 && j <= c - 1) Z.st(j, c, mk(0.0, 0.0));
+            __syncwarp();
+        }
+        if (j <= n) {
+            Z.st(j, 1, mk(j == 1 ? 1.0 : 0.0, 0.0));
+            if (j > 1) Z.st(1, j, mk(0.0, 0.0));
+        }
+        if (j <= n)  // clear below the subdiagonal
+            for (int k = j + 2; k <= n; ++k) H.st(k, j, mk(0.0, 0.0));
+        __syncwarp();
+
+        if (!(status & ST_NONFINITE)) {
+            // ---- make the subdiagonal real
+            for (int i = 2; i <= n; ++i) {
+                const cx<double> h = H.ld(i, i - 1);
+                if (h.i != 0.0) {
+                    cx<double> sc = cscal(h, 1.0 / cabs1(h));
+                    sc = cscal(conj(sc), 1.0 / cabs(sc));
+                    __syncwarp();
+                    if (lane == 0) H.st(i, i - 1, mk(cabs(h), 0.0));
+                    if (j >= i && j <= n) H.st(i, j, cmul(H.ld(i, j), sc));
+                    __syncwarp();
+                    const int re = (i + 1) < n ? (i + 1) : n;
+                    if (j <= re) H.st(j, i, cmulc(H.ld(j, i), sc));
+                    if (j <= n) Z.st(j, i, cmulc(Z.ld(j, i), sc));
+                }
+                __syncwarp();
+            }
+            // ---- single-shift QR
+            int I = n, L = 1, its = 0;
+            while (I > 1) {
+                if (its > a.max_its) { status |= ST_ITCAP; --I; L = 1; its = 0; continue; }
+                L = deflation_scan<double>(I, L, H, n, ulp, smlnum);
+                __syncwarp();
+                if (L > 1 && lane == 0) H.st(L, L - 1, mk(0.0, 0.0));
+                __syncwarp();
+                if (L >= I) { --I; L = 1; its = 0; continue; }
+                const cx<double> t = qr_shift<double>(I, L, its, H);
+                const cx<double> h11s = csub(H.ld(L, L), t);
+                const double h21 = H.ld(L + 1, L).r;
+                const double rs = 1.0 / (cabs1(h11s) + fabs(h21));
+                const cx<double> v0 = cscal(h11s, rs), v1 = mk(h21 * rs, 0.0);
+                ++its;
+                ++sweeps;
+                for (int K = L; K <= I - 1; ++K) {
+                    cx<double> a0 = v0, a1 = v1, t1;
+                    if (K > L) { a0 = H.ld(K, K - 1); a1 = H.ld(K + 1, K - 1); }
+                    zlarfg2<double>(a0, a1, t1);
+                    __syncwarp();
+                    if (K > L && lane == 0) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(0.0, 0.0)); }
+                    const cx<double> w1 = a1, c1 = conj(t1), cw = conj(w1);
+                    const double t2 = fma(t1.r, w1.r, -(t1.i * w1.i));
+                    if (j <= n) {  // Schur vectors: row j of columns K, K+1; H: rows K, K+1 of column j >= K
+                        cx<double> z1 = Z.ld(j, K), z2 = Z.ld(j, K + 1);
+                        rot_pair(z1, z2, t1, t2, cw);
+                        Z.st(j, K, z1);
+                        Z.st(j, K + 1, z2);
+                        if (j >= K) {
+                            cx<double> h1 = H.ld(K, j), h2 = H.ld(K + 1, j);
+                            rot_pair(h1, h2, c1, t2, w1);
+                            H.st(K, j, h1);
+                            H.st(K + 1, j, h2);
+                        }
+                    }
+                    __syncwarp();
+                    const int je = (K + 2) < I ? (K + 2) : I;
+                    if (j <= je) {  // columns K, K+1, row j
+                        cx<double> h1 = H.ld(j, K), h2 = H.ld(j, K + 1);
+                        rot_pair(h1, h2, t1, t2, cw);
+                        H.st(j, K, h1);
+                        H.st(j, K + 1, h2);
+                    }
+                    __syncwarp();
+                }
+                // make H(I, I-1) real
+                const cx<double> h = H.ld(I, I - 1);
+                if (h.i != 0.0) {
+                    const double d = cabs(h);
+                    const cx<double> z = conj(cscal(h, 1.0 / d));
+                    __syncwarp();
+                    if (lane == 0) H.st(I, I - 1, mk(d, 0.0));
+                    if (j >= I + 1 && j <= n) H.st(I, j, cmul(H.ld(I, j), z));
+                    if (j <= I - 1) H.st(j, I, cmulc(H.ld(j, I), z));
+                    if (j <= n) Z.st(j, I, cmulc(Z.ld(j, I), z));
+                }
+                __syncwarp();
+            }
+        }
+
+        // ---- eigenvalues, Schur form, eigenvectors
+        const VecSoA<double> E{a.rE + vo, a.iE + vo, a.g.tc};
+        if (j <= n) E.st(j, H.ld(j, j));
+        if (a.rT) {
+            const MatSoA<double> T{a.rT + mo, a.iT + mo, tc, n};
+            if (j <= n)
+                for (int i = 1; i <= n; ++i) T.st(i, j, i <= j ? H.ld(i, j) : mk(0.0, 0.0));
+        }
+        if (j >= 2 && j <= n) {  // T-eigenvector j (back substitution) into column j of X
+            const cx<double> tkk = H.ld(j, j);
+            const double smin = fmax(ulp * cabs1(tkk), smlnum);
+            const double s = trevc_solve<double>(j, H, SmemCol64{fsm + 2 * n * lda + (j - 1) * lda}, smin, tkk);
+            sS[j - 1] = make_double2(s, 0.0);
+        }
+        __syncwarp();
+        if (j <= n) {  // row j of Z := Z [x; s; 0], columns n down to 2 (Z(j, 1:ki-1) still Q's)
+            for (int ki = n; ki >= 2; --ki) {
+                cx<double> acc = Z.ld(j, ki);
+                const double s = sS[ki - 1].x;
+                if (s != 1.0) acc = cscal(acc, s);
+                for (int q = 1; q <= ki - 1; ++q) acc = cmac(acc, Z.ld(j, q), X.ld(q, ki));
+                Z.st(j, ki, acc);
+            }
+        }
+        __syncwarp();
+        if (j <= n) {
+            const MatSoA<double> V{a.rV + mo, a.iV + mo, tc, n};
+            const double scale = vector_scale<double>(n, Z, j, a.vnorm);
+            for (int i = 1; i <= n; ++i) V.st(i, j, cscal(Z.ld(i, j), scale));
+        }
+        if (lane == 0) {
+            if (a.status) a.status[m] = status | (a.list ? ST_REFINE_FALLBACK : 0);
+            if (a.sweeps) a.sweeps[m] = sweeps;
+        }
+        __syncwarp();
     }
 }
 
@@ -483,6 +734,26 @@ cudaError_t launch_polish32(Geom g, const double *rA, const double *iA, const do
     return cudaGetLastError();
 }
 
+cudaError_t launch_fp64_list(FusedArgs a, cudaStream_t st)
+{
+    if (a.g.N <= 0) return cudaSuccess;
+    a.list_split = 0;
+    if (a.list && !a.rS && a.g.n <= 32) {
+        // per call (per device, thread safe; microseconds next to the kernel)
+        cudaError_t e = cudaFuncSetAttribute(fp64_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)fp64_warp_smem(32));
+        if (e != cudaSuccess) return e;
+        int per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fp64_warp_kernel, 32, fp64_warp_smem(a.g.n));
+        const long long slots = (long long)device_sms() * std::max(per_sm, 1);
+        a.list_split = std::min<long long>(a.g.N, slots);
+        fp64_warp_kernel<<<(unsigned)a.list_split, 32, fp64_warp_smem(a.g.n), st>>>(a);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return launch_fused_fp64(a, st);
+}
+
 cudaError_t launch_fused_fp64_blocks(const FusedArgs &a, int blocks, cudaStream_t st)
 {
     if (a.g.N <= 0) return cudaSuccess;
@@ -575,6 +846,7 @@ void load_fused_kernels()
 {
     load_kernel(fused_fp64_kernel<false>);
     load_kernel(fused_fp64_kernel<true>);
+    load_kernel(fp64_warp_kernel);
     load_kernel(polish32_warp_kernel);
     load_kernel(zgehrd_kernel);
     load_kernel(zunghr_kernel);

@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
                     __syncwarp(gmask);
                     if (K > L && gl == 0) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(0.f, 0.f)); }
                     const cx<float> w1 = a1, cw = conj(w1), c1 = conj(t1);
-                    const float t2 = t1.r * w1.r - t1.i * w1.i;
+                    const float t2 = fmaf(t1.r, w1.r, -(t1.i * w1.i));
                     if (j >= K && j <= n) {  // rows K, K+1, column j
                         cx<float> h1 = H.ld(K, j), h2 = H.ld(K + 1, j);
                         rot_pair(h1, h2, c1, t2, w1);
