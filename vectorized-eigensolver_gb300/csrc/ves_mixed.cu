@@ -23,7 +23,7 @@
 // "Improving the accuracy of computed eigenvalues and eigenvectors", SIAM J.
 // Numer. Anal. 20 (1983)).  With the FP32 Schur form A ~ Z T Z^H and the
 // T-eigenvector x (x_i = 0 for i > k):
-//     r    = A v - lambda v                    FP64
+//     r    = A v - lambda v                    FP64 (the first one in float-float)
 //     r'   = Z^H r                             FP32
 //     (T - lambda I) dx - dlambda x = -r', dx_k = 0:
 //        rows i > k : back substitution for dx_i
@@ -56,8 +56,10 @@ __device__ __forceinline__ long long soa_off_m(long long m, long long len, int t
     return (m / tc) * (long long)tc * len + (m % tc);
 }
 
-// float2 elements per group of 32 matrices: T, Z, X (n*n each), work (n).
-__host__ __device__ __forceinline__ long long group_elems(int n) { return 3LL * n * n + n; }
+// float2 elements per group of 32 matrices: T, Z, X (n*n each), work (n),
+// then A as two FP32 parts Ah + Al (n*n each; A - Ah - Al ~ 2^-48 |A|) for
+// the refinement's first residual.
+__host__ __device__ __forceinline__ long long group_elems(int n) { return 5LL * n * n + n; }
 
 // T-eigenvectors: column k of X solves (T(1:k-1,1:k-1) - T(k,k) I) x = -T(1:k-1,k)
 // with the unit entry at k (the reference's ztrevc back substitution,
@@ -81,6 +83,25 @@ __device__ void trevc_x_lane(const int n, const MT &T, typename vec2<R>::T *pX)
 __device__ __forceinline__ cx<double> up(cx<float> z) { return mk((double)z.r, (double)z.i); }
 __device__ __forceinline__ cx<float> down(cx<double> z) { return mk((float)z.r, (float)z.i); }
 
+// Float-float accumulation (the first residual): s + p exactly as s' + e
+// (TwoSum, Knuth), and s + a*b with the product's rounding error (exact, by
+// fma) carried in e.  The _rn intrinsics keep the compiler from fusing these
+// operations, which would void the exactness.
+__device__ __forceinline__ void two_sum_acc(float &s, float &e, const float p)
+{
+    const float t = __fadd_rn(s, p);
+    const float bp = __fsub_rn(t, s);
+    e = __fadd_rn(e, __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp)));
+    s = t;
+}
+__device__ __forceinline__ void ff_mac(float &s, float &e, const float a, const float b)
+{
+    const float pr = __fmul_rn(a, b);
+    const float pe = fmaf(a, b, -pr);
+    two_sum_acc(s, e, pr);
+    e = __fadd_rn(e, pe);
+}
+
 __device__ __forceinline__ void to_fp64_list(const MixedArgs &a, int *flags, long long m)
 {
     // the first pair (or the Schur kernel) to give up on matrix m puts it on the list
@@ -101,6 +122,7 @@ __global__ void __launch_bounds__(kSchurThreads) schur32_kernel(const MixedArgs 
         float2 *pZ = pT + 32 * nn, *pX = pZ + 32 * nn, *pW = pX + 32 * nn;
         const MatIlv<float> T{pT, n}, Z{pZ, n};
         const VecIlv<float> W{pW};
+        const MatIlv<float> Ah{pW + 32 * n, n}, Al{pW + 32 * (n + nn), n};
         const long long m = g * 32 + lane;
         const bool valid = m >= a.m_begin && m < a.m_end;
         int status = 0, sweeps = 0;
@@ -117,6 +139,8 @@ __global__ void __launch_bounds__(kSchurThreads) schur32_kernel(const MixedArgs 
                     const cx<float> f = down(v);
                     nA2 = fma(f.i, f.i, fma(f.r, f.r, nA2));
                     T.st(i, j, f);
+                    Ah.st(i, j, f);
+                    Al.st(i, j, down(csub(v, up(f))));
                 }
             fb = bad || !(nA2 < 1e36f);  // beyond FP32 range: FP64
             zgehrd_lane<float>(n, T, W);
@@ -155,9 +179,9 @@ __global__ void __launch_bounds__(kSchurThreads) schur32_kernel(const MixedArgs 
 // ---------------------------------------------------------------------------
 constexpr int kWarpSchurThreads = 128;  // 4 warps per block
 
-// per-matrix buffer layout: T, Z, X (n*n float2 each, column-major), then a
-// work vector whose first entry holds ||A||_F^2
-__host__ __device__ __forceinline__ long long mat_elems(int n) { return 3LL * n * n + n; }
+// per-matrix buffer layout: T, Z, X (n*n float2 each, column-major), a work
+// vector whose first entry holds ||A||_F^2, then Ah and Al (n*n each)
+__host__ __device__ __forceinline__ long long mat_elems(int n) { return 5LL * n * n + n; }
 
 __host__ __device__ __forceinline__ size_t warp_schur_smem(int n, int G)
 {
@@ -186,6 +210,7 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
     for (long long m = a.m_begin + gw; m < a.m_end; m += nw) {
         // ---- load A (FP64 SoA) into H as FP32; non-finite / out-of-range check
         const long long mo = soa_off_m(m, nn, tc);
+        float2 *oA = buf + m * mat_elems(n) + 3 * nn + n;  // Ah, Al of the per-matrix layout
         bool bad = false;
         float s2 = 0.f;
         for (int e = gl; e < nn; e += G) {
@@ -195,6 +220,8 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
             const float fr = (float)re, fi = (float)im;
             s2 = fmaf(fi, fi, fmaf(fr, fr, s2));
             sH[(e % n) + (e / n) * lda] = make_float2(fr, fi);
+            oA[e] = make_float2(fr, fi);
+            oA[nn + e] = make_float2((float)(re - (double)fr), (float)(im - (double)fi));
         }
         const float nA2 = group_sum<G>(s2, gmask);
         bool fb = __any_sync(gmask, bad) || !(nA2 < 1e36f);
@@ -368,6 +395,7 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
     float2 *pT = const_cast<float2 *>(buf) +
                  (kPerMatrix ? m * mat_elems(n) : (m / 32) * group_elems(n) * 32 + (m % 32));
     const MatBuf<S> T{pT, n}, Z{pT + S * nn, n}, X{pT + 2 * S * nn, n};
+    const MatBuf<S> Ah{pT + S * (3 * nn + n), n}, Al{pT + S * (4 * nn + n), n};
     const float nA2 = pT[3 * S * nn].x;
     const long long mo = soa_off_m(m, nn, tc);
     const MatSoA<double> A{const_cast<double *>(a.rA) + mo, const_cast<double *>(a.iA) + mo, tc, n};
@@ -381,6 +409,7 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
             cx<float> acc = mk(0.f, 0.f);
             for (int j = 1; j <= k; ++j) acc = cmac(acc, Z.ld(i, j), X.ld(j, k));
             v[i - 1] = up(acc);
+            dx[i - 1] = acc;  // v0 in FP32 for the first residual (dx is free until then)
         }
     }
     const double tol2 = a.tol * a.tol;
@@ -392,17 +421,46 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
     for (int step = 0; step <= a.max_steps; ++step) {
         if (!__any_sync(FULL, act)) break;
         if (!act) continue;
-        // FP64 residual
-        double rn2 = 0.0, vn2 = 0.0;
-        for (int i = 1; i <= n; ++i) {
-            const cx<double> vi = v[i - 1];
-            cx<double> acc = mk(-(lam.r * vi.r - lam.i * vi.i), -(lam.r * vi.i + lam.i * vi.r));
-            for (int j = 1; j <= n; ++j) acc = cmac(acc, A.ld(i, j), v[j - 1]);
-            rn2 = fma(acc.i, acc.i, fma(acc.r, acc.r, rn2));
-            vn2 = fma(vi.i, vi.i, fma(vi.r, vi.r, vn2));
-            r32[i - 1] = down(acc);
+        bool certified = false;
+        if (step == 0) {
+            // First residual in float-float on the FP32 pipe: v0 and lambda0 are
+            // FP32 numbers and A = Ah + Al, so every product splits exactly into
+            // a rounded product and its error; the rounded products are summed
+            // by TwoSum, the rest in FP32.  Error ~ 2^-48 ||A|| ||v||, far below
+            // what the first correction needs (its result is ~1e-14 off from the
+            // FP32 solve anyway); it is never used to accept a pair.
+            const cx<float> l0 = T.ld(k, k);
+            for (int i = 1; i <= n; ++i) {
+                const cx<float> vi = dx[i - 1];
+                float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f;
+                ff_mac(sr, er, -l0.r, vi.r);
+                ff_mac(sr, er, l0.i, vi.i);
+                ff_mac(si, ei, -l0.r, vi.i);
+                ff_mac(si, ei, -l0.i, vi.r);
+                for (int j = 1; j <= n; ++j) {
+                    const cx<float> ah = Ah.ld(i, j), al = Al.ld(i, j), vj = dx[j - 1];
+                    ff_mac(sr, er, ah.r, vj.r);
+                    ff_mac(sr, er, -ah.i, vj.i);
+                    ff_mac(si, ei, ah.r, vj.i);
+                    ff_mac(si, ei, ah.i, vj.r);
+                    er = fmaf(-al.i, vj.i, fmaf(al.r, vj.r, er));
+                    ei = fmaf(al.i, vj.r, fmaf(al.r, vj.i, ei));
+                }
+                r32[i - 1] = mk(__fadd_rn(sr, er), __fadd_rn(si, ei));
+            }
+        } else {
+            // FP64 residual: the one that accepts
+            double rn2 = 0.0, vn2 = 0.0;
+            for (int i = 1; i <= n; ++i) {
+                const cx<double> vi = v[i - 1];
+                cx<double> acc = mk(-(lam.r * vi.r - lam.i * vi.i), -(lam.r * vi.i + lam.i * vi.r));
+                for (int j = 1; j <= n; ++j) acc = cmac(acc, A.ld(i, j), v[j - 1]);
+                rn2 = fma(acc.i, acc.i, fma(acc.r, acc.r, rn2));
+                vn2 = fma(vi.i, vi.i, fma(vi.r, vi.r, vn2));
+                r32[i - 1] = down(acc);
+            }
+            certified = rn2 <= tol2 * (double)nA2 * vn2;
         }
-        const bool certified = rn2 <= tol2 * (double)nA2 * vn2;
         if (!certified && step == a.max_steps) { fail = true; act = false; continue; }
         // FP32 correction through the Schur form: r' = Z^H r kept in dx
         for (int i = 1; i <= n; ++i) {
