@@ -327,7 +327,7 @@ LEARNED = {
     32: dict(net=dict(hidden=256, layers=5, fourier=12, loss=1, delta=0.01), epochs=300, polish=10, gate=3e-2),
     # 1,048,576 x 24x24: the network as specified for this workload (inputs: the 3
     # parameters and the 24 complex diagonal entries; 3 hidden layers of 256, GELU)
-    24: dict(net=dict(hidden=256, layers=3, fourier=0, loss=1, delta=0.01), epochs=40, polish=6, gate=3e-2),
+    24: dict(net=dict(hidden=256, layers=3, fourier=0, loss=1, delta=0.01), epochs=150, polish=10, gate=3e-2),
 }
 
 
