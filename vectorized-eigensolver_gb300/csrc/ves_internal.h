@@ -74,7 +74,7 @@ cudaError_t launch_mixed(const MixedArgs &a, cudaStream_t st);
 cudaError_t launch_mixed_overlap(const MixedArgs &a, cudaStream_t st, cudaStream_t s_schur, cudaStream_t s_refine);
 
 // Fused zgehrd -> zunghr -> zlahqr -> ztrevc, FP64.
-// blocks_per_sm = 0 takes the library default (VES_FUSED_BLOCKS_PER_SM, else 2).
+// blocks_per_sm = 0 takes the library default (VES_FUSED_BLOCKS_PER_SM, else 4; 3 for 21 <= n <= 28).
 // learned = the shift-seeded kernel, whose slots also hold an FP32 copy of H
 // and the n predictions.
 size_t fused_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blocks, int *out_threads,

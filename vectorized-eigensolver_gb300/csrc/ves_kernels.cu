@@ -668,14 +668,18 @@ __global__ void fp64_fma_probe_kernel(double *out, int iters, double b, double c
 constexpr int kStageThreads = 128;
 inline unsigned stage_blocks(const Geom &g) { return (unsigned)((g.N + kStageThreads - 1) / kStageThreads); }
 
-// default blocks (4 warps each) per SM: 8 warps; VES_FUSED_BLOCKS_PER_SM overrides
-int fused_default_bps()
+// Blocks (4 warps) per SM of the persistent FP64 grid when the caller leaves
+// it to the library; VES_FUSED_BLOCKS_PER_SM overrides.  Measured on GB300
+// (eigensolves/s, 2 -> 3 -> 4 -> 5 blocks): n=8 8.88 9.07 9.19 9.30 M/s,
+// n=16 1.588 1.651 1.656 1.637 M/s, n=24 0.520 0.565 0.549 0.546 M/s,
+// n=32 0.230 0.248 0.251 0.232 M/s, n=48 0.063 0.060 0.068 0.068 M/s.
+int fused_default_bps(int n)
 {
     if (const char *e = getenv("VES_FUSED_BLOCKS_PER_SM")) {
         const int v = atoi(e);
         if (v >= 1 && v <= 16) return v;
     }
-    return 2;
+    return (n >= 21 && n <= 28) ? 3 : 4;
 }
 
 int device_sms()
@@ -693,7 +697,7 @@ size_t fused_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blo
     const int sms = device_sms();
     const long long groups = (N + 31) / 32;
     const int wpb = kFusedThreads / 32;
-    const int bps = blocks_per_sm > 0 ? blocks_per_sm : fused_default_bps();
+    const int bps = blocks_per_sm > 0 ? blocks_per_sm : fused_default_bps(n);
     long long blocks = std::min<long long>((groups + wpb - 1) / wpb, (long long)sms * bps);
     if (blocks < 1) blocks = 1;
     const size_t per_slot = (size_t)fused_slot_elems(n, learned) * 32 * sizeof(double2);
