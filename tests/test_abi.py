@@ -41,6 +41,17 @@ def test_version():
     assert ves.lib().ves_version() >= 100
 
 
+def test_default_options_match_the_header():
+    """ves_default_options (host code) gives the defaults include/ves.h documents."""
+    o = ves.default_options()
+    assert o.precision == ves.VES_PREC_FP64
+    assert o.max_its == 30
+    assert o.refine_steps == 8
+    assert o.refine_tol == 5e-14
+    assert o.want_vectors == 1
+    assert o.blocks_per_sm == 0  # the library's measured launch shape
+
+
 def _soa_reference(A, tc):
     N, n, _ = A.shape
     out = np.zeros(N * n * n)
