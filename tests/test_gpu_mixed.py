@@ -47,13 +47,14 @@ def test_mixed_matches_oracle(n, N, tc):
 
 @pytest.mark.parametrize("n,N,tc,vnorm", [(10, 96, 32, 0), (1, 64, 32, 0), (2, 96, 8, 0), (5, 160, 32, 1),
                                          (16, 96, 32, 2), (24, 64, 16, 0), (32, 96, 32, 1), (40, 64, 32, 0),
-                                         (16, 5000, 40, 0), (32, 5120, 512, 2)])
+                                         (64, 64, 32, 1), (16, 5000, 40, 0), (32, 5120, 512, 2), (48, 1000, 40, 2)])
 def test_mixed_forced_fallback_equals_fp64(n, N, tc, vnorm):
     """With no Newton step allowed nothing can be certified: every matrix goes
     through the FP64 solver and the result is the plain FP64 result bit for
-    bit, sweep counts included.  For n <= 32 the first list entries (one per
-    warp slot of the GPU) go to the warp-per-matrix FP64 kernel and the rest
-    (N = 5000, 5120) to the lane kernel; n = 40 is the lane kernel only."""
+    bit, sweep counts included.  The first list entries (one per warp slot of
+    the GPU) go to the warp-per-matrix FP64 kernel (a lane owns two rows and
+    columns for n > 32) and the rest (N = 5000, 5120, 1000) to the lane
+    kernel."""
     rng = np.random.default_rng(3 + n)
     A = cgauss(rng, (N, n, n))
     A[3] = np.triu(A[3])  # already triangular: the reflectors' trivial branch

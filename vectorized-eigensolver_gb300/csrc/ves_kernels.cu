@@ -177,13 +177,13 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
 
 // ---------------------------------------------------------------------------
 // fp64_warp_kernel: the fused kernel's FP64 solve (no learned shifts) for
-// n <= 32 with one matrix per warp, H, Z and the T-eigenvectors X in shared
-// memory; for the few matrices on a device list (those the FP32+refine form
+// n <= 64 with one matrix per warp, H, Z and the T-eigenvectors X in shared
+// memory (197 KB at n = 64); for the few matrices on a device list (those the FP32+refine form
 // hands back to FP64).  The lane kernel solves such a list in one or two
 // lanes of one warp, and an FP64 warp instruction costs the same with one
 // active lane as with 32: 11 ms at n = 16 and 72 ms at n = 32 on GB300 for
-// one or two matrices.  Here lane l owns row l + 1 of a column operation and
-// column l + 1 of a row operation (as in schur32_warp_kernel), and each
+// one or two matrices.  Here lane l owns rows l + 1 and l + 33 of a column
+// operation and the same columns of a row operation, and each
 // element goes through the same operations in the same order as in the lane
 // routines (zgehrd_lane, zunghr_lane, clear_below_subdiag_lane,
 // make_subdiag_real_lane, zlahqr_warp, ztrevc_lane, write_vectors), the
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(32) fp64_warp_kernel(const FusedArgs a)
 {
     extern __shared__ double2 fsm[];
     const int n = a.g.n, tc = a.g.tc;
-    const int lane = threadIdx.x, j = lane + 1;  // the row / column this lane owns
+    const int lane = threadIdx.x;  // owns rows / columns lane + 1 and lane + 33 (n <= 64)
     const int lda = n + 1;
     const SmemMat64 H{fsm, lda}, Z{fsm + n * lda, lda}, X{fsm + 2 * n * lda, lda};
     double2 *sTau = fsm + 3 * n * lda, *sS = sTau + n;
@@ -254,10 +254,10 @@ __global__ void __launch_bounds__(32) fp64_warp_kernel(const FusedArgs a)
                 scale = cinv(mk(alpha.r - beta, alpha.i));
             }
             __syncwarp();  // every lane has read column i
-            if (j >= i + 2 && j <= n) H.st(j, i, cmul(H.ld(j, i), scale));
+            for (int j = lane + 1; j <= n; j += 32) if (j >= i + 2 && j <= n) H.st(j, i, cmul(H.ld(j, i), scale));
             if (lane == 0) sTau[i - 1] = make_double2(t.r, t.i);
             __syncwarp();
-            if (j <= n) {  // right: row j of A(1:n, i+1:n) -= tau (A v)_j v^H
+            for (int j = lane + 1; j <= n; j += 32) if (j <= n) {  // right: row j of A(1:n, i+1:n) -= tau (A v)_j v^H
                 cx<double> sacc = H.ld(j, i + 1);
                 for (int q = 2; q <= mm; ++q) sacc = cmac(sacc, H.ld(j, i + q), H.ld(i + q, i));
                 const cx<double> ts = cmul(t, sacc);
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(32) fp64_warp_kernel(const FusedArgs a)
                 for (int q = 2; q <= mm; ++q) H.st(j, i + q, cnmacc(H.ld(j, i + q), ts, H.ld(i + q, i)));
             }
             __syncwarp();
-            if (j >= i + 1 && j <= n) {  // left: column j of A(i+1:n, i+1:n) -= conj(tau) v (v^H A)_j
+            for (int j = lane + 1; j <= n; j += 32) if (j >= i + 1 && j <= n) {  // left: column j of A(i+1:n, i+1:n) -= conj(tau) v (v^H A)_j
                 const cx<double> tcj = conj(t);
                 cx<double> sacc = H.ld(i + 1, j);
                 for (int q = 2; q <= mm; ++q) sacc = cjmac(sacc, H.ld(i + q, i), H.ld(i + q, j));
@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(32) fp64_warp_kernel(const FusedArgs a)
         for (int i = n - 1; i >= 1; --i) {
             const cx<double> t = mk(sTau[i - 1].x, sTau[i - 1].y);
             const int c = i + 1;
-            if (j >= c + 1 && j <= n) {
+            for (int j = lane + 1; j <= n; j += 32) if (j >= c + 1 && j <= n) {
                 cx<double> sacc = Z.ld(c, j);
                 for (int k = c + 1; k <= n; ++k) sacc = cjmac(sacc, H.ld(k, i), Z.ld(k, j));
                 const cx<double> ts = cmul(t, sacc);
@@ -290,16 +290,16 @@ __global__ void __launch_bounds__(32) fp64_warp_kernel(const FusedArgs a)
             }
             __syncwarp();
             const cx<double> mt = mk(-t.r, -t.i);
-            if (j >= c + 1 && j <= n) Z.st(j, c, cmul(H.ld(j, i), mt));
-            if (j == c) Z.st(c, c, mk(1.0 - t.r, -t.i));
-            if (j >= 2 && j <= c - 1) Z.st(j, c, mk(0.0, 0.0));
+            for (int j = lane + 1; j <= n; j += 32) if (j >= c + 1 && j <= n) Z.st(j, c, cmul(H.ld(j, i), mt));
+            for (int j = lane + 1; j <= n; j += 32) if (j == c) Z.st(c, c, mk(1.0 - t.r, -t.i));
+            for (int j = lane + 1; j <= n; j += 32) if (j >= 2 && j <= c - 1) Z.st(j, c, mk(0.0, 0.0));
             __syncwarp();
         }
-        if (j <= n) {
+        for (int j = lane + 1; j <= n; j += 32) if (j <= n) {
             Z.st(j, 1, mk(j == 1 ? 1.0 : 0.0, 0.0));
             if (j > 1) Z.st(1, j, mk(0.0, 0.0));
         }
-        if (j <= n)  // clear below the subdiagonal
+        for (int j = lane + 1; j <= n; j += 32) if (j <= n)  // clear below the subdiagonal
             for (int k = j + 2; k <= n; ++k) H.st(k, j, mk(0.0, 0.0));
         __syncwarp();
 
@@ -312,11 +312,11 @@ __global__ void __launch_bounds__(32) fp64_warp_kernel(const FusedArgs a)
                     sc = cscal(conj(sc), 1.0 / cabs(sc));
                     __syncwarp();
                     if (lane == 0) H.st(i, i - 1, mk(cabs(h), 0.0));
-                    if (j >= i && j <= n) H.st(i, j, cmul(H.ld(i, j), sc));
+                    for (int j = lane + 1; j <= n; j += 32) if (j >= i && j <= n) H.st(i, j, cmul(H.ld(i, j), sc));
                     __syncwarp();
                     const int re = (i + 1) < n ? (i + 1) : n;
-                    if (j <= re) H.st(j, i, cmulc(H.ld(j, i), sc));
-                    if (j <= n) Z.st(j, i, cmulc(Z.ld(j, i), sc));
+                    for (int j = lane + 1; j <= n; j += 32) if (j <= re) H.st(j, i, cmulc(H.ld(j, i), sc));
+                    for (int j = lane + 1; j <= n; j += 32) if (j <= n) Z.st(j, i, cmulc(Z.ld(j, i), sc));
                 }
                 __syncwarp();
             }
@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(32) fp64_warp_kernel(const FusedArgs a)
                     if (K > L && lane == 0) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(0.0, 0.0)); }
                     const cx<double> w1 = a1, c1 = conj(t1), cw = conj(w1);
                     const double t2 = fma(t1.r, w1.r, -(t1.i * w1.i));
-                    if (j <= n) {  // Schur vectors: row j of columns K, K+1; H: rows K, K+1 of column j >= K
+                    for (int j = lane + 1; j <= n; j += 32) if (j <= n) {  // Schur vectors: row j of columns K, K+1; H: rows K, K+1 of column j >= K
                         cx<double> z1 = Z.ld(j, K), z2 = Z.ld(j, K + 1);
                         rot_pair(z1, z2, t1, t2, cw);
                         Z.st(j, K, z1);
@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(32) fp64_warp_kernel(const FusedArgs a)
                     }
                     __syncwarp();
                     const int je = (K + 2) < I ? (K + 2) : I;
-                    if (j <= je) {  // columns K, K+1, row j
+                    for (int j = lane + 1; j <= n; j += 32) if (j <= je) {  // columns K, K+1, row j
                         cx<double> h1 = H.ld(j, K), h2 = H.ld(j, K + 1);
                         rot_pair(h1, h2, t1, t2, cw);
                         H.st(j, K, h1);
@@ -373,9 +373,9 @@ __global__ void __launch_bounds__(32) fp64_warp_kernel(const FusedArgs a)
                     const cx<double> z = conj(cscal(h, 1.0 / d));
                     __syncwarp();
                     if (lane == 0) H.st(I, I - 1, mk(d, 0.0));
-                    if (j >= I + 1 && j <= n) H.st(I, j, cmul(H.ld(I, j), z));
-                    if (j <= I - 1) H.st(j, I, cmulc(H.ld(j, I), z));
-                    if (j <= n) Z.st(j, I, cmulc(Z.ld(j, I), z));
+                    for (int j = lane + 1; j <= n; j += 32) if (j >= I + 1 && j <= n) H.st(I, j, cmul(H.ld(I, j), z));
+                    for (int j = lane + 1; j <= n; j += 32) if (j <= I - 1) H.st(j, I, cmulc(H.ld(j, I), z));
+                    for (int j = lane + 1; j <= n; j += 32) if (j <= n) Z.st(j, I, cmulc(Z.ld(j, I), z));
                 }
                 __syncwarp();
             }
@@ -383,20 +383,20 @@ __global__ void __launch_bounds__(32) fp64_warp_kernel(const FusedArgs a)
 
         // ---- eigenvalues, Schur form, eigenvectors
         const VecSoA<double> E{a.rE + vo, a.iE + vo, a.g.tc};
-        if (j <= n) E.st(j, H.ld(j, j));
+        for (int j = lane + 1; j <= n; j += 32) if (j <= n) E.st(j, H.ld(j, j));
         if (a.rT) {
             const MatSoA<double> T{a.rT + mo, a.iT + mo, tc, n};
-            if (j <= n)
+            for (int j = lane + 1; j <= n; j += 32) if (j <= n)
                 for (int i = 1; i <= n; ++i) T.st(i, j, i <= j ? H.ld(i, j) : mk(0.0, 0.0));
         }
-        if (j >= 2 && j <= n) {  // T-eigenvector j (back substitution) into column j of X
+        for (int j = lane + 1; j <= n; j += 32) if (j >= 2 && j <= n) {  // T-eigenvector j (back substitution) into column j of X
             const cx<double> tkk = H.ld(j, j);
             const double smin = fmax(ulp * cabs1(tkk), smlnum);
             const double s = trevc_solve<double>(j, H, SmemCol64{fsm + 2 * n * lda + (j - 1) * lda}, smin, tkk);
             sS[j - 1] = make_double2(s, 0.0);
         }
         __syncwarp();
-        if (j <= n) {  // row j of Z := Z [x; s; 0], columns n down to 2 (Z(j, 1:ki-1) still Q's)
+        for (int j = lane + 1; j <= n; j += 32) if (j <= n) {  // row j of Z := Z [x; s; 0], columns n down to 2 (Z(j, 1:ki-1) still Q's)
             for (int ki = n; ki >= 2; --ki) {
                 cx<double> acc = Z.ld(j, ki);
                 const double s = sS[ki - 1].x;
@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(32) fp64_warp_kernel(const FusedArgs a)
             }
         }
         __syncwarp();
-        if (j <= n) {
+        for (int j = lane + 1; j <= n; j += 32) if (j <= n) {
             const MatSoA<double> V{a.rV + mo, a.iV + mo, tc, n};
             const double scale = vector_scale<double>(n, Z, j, a.vnorm);
             for (int i = 1; i <= n; ++i) V.st(i, j, cscal(Z.ld(i, j), scale));
@@ -742,10 +742,10 @@ cudaError_t launch_fp64_list(FusedArgs a, cudaStream_t st)
 {
     if (a.g.N <= 0) return cudaSuccess;
     a.list_split = 0;
-    if (a.list && !a.rS && a.g.n <= 32) {
+    if (a.list && !a.rS && a.g.n <= 64) {
         // per call (per device, thread safe; microseconds next to the kernel)
         cudaError_t e = cudaFuncSetAttribute(fp64_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)fp64_warp_smem(32));
+                                             (int)fp64_warp_smem(64));
         if (e != cudaSuccess) return e;
         int per_sm = 1;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fp64_warp_kernel, 32, fp64_warp_smem(a.g.n));
