@@ -81,7 +81,7 @@ size_t fused_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blo
                              bool learned = false);
 cudaError_t launch_fused_fp64(const FusedArgs &a, cudaStream_t st);
 // The FP64 solve of the matrices on a.list: the first entries (one per warp
-// slot of the GPU) by fp64_warp_kernel (one matrix per warp, n <= 32), the
+// slot of the GPU) by fp64_warp_kernel (one matrix per warp, n <= 64), the
 // rest by the lane kernel; the same results bit for bit either way.
 cudaError_t launch_fp64_list(FusedArgs a, cudaStream_t st);
 
