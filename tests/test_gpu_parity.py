@@ -1,7 +1,7 @@
 """Parity of the sm_103a eigensolver (libves.so) with the oracle and with the
 reference's own outputs.
 
-Tolerances (the spec bar for floating point):
+Tolerances (the bar every form meets, floating point):
   eigenvalues, after optimal matching:      |lambda - lambda_ref| <= 1e-12 * ||A||_F
   normalised residual per eigenpair:        ||A v - lambda v|| / (||A||_F ||v||) <= 1e-13
 Eigenvectors are compared up to a unit phase (the Schur basis is unique only
