@@ -37,6 +37,15 @@ forms   the other forms, each on its own batch, each verified (residuals on the
         mixed-size   500,000 matrices of orders 4..64 (Gaussian, non-normal,
                      clustered; seed 2): one CUDA-graph replay of the binned
                      persistent solve against one launch per order.
+        Each form entry carries its own roofline from its algorithmic work
+        (device-counted where it is data dependent: QR sweeps, Newton
+        corrections and residuals of the refinement, polish steps): FP64
+        flops against the FP64 FMA rate probed in this run, FP32 flops
+        against the FP32 FMA rate probed in this run, BF16 tensor flops
+        against MEASURED_PEAKS.json's bf16_tflops, and 32 n^2 + 16 n bytes per
+        matrix against its hbm_gbs; `bound` names the unit whose work takes
+        longest at its peak.  The JSON line keeps each form compact; the full
+        record of each form is printed to stderr.
 Every result is verified after timing: all residuals on the device in FP64
 (<= 1e-13 of ||A||_F ||v||); eigenvalue parity with the oracle is the job of
 the test suite (tests/test_gpu_fullsize.py runs this workload).
@@ -66,9 +75,48 @@ METRIC = "eigensolves/s at n=16,32 at resid≤1e-13; learned-shift, FP32+refine 
 WORKLOAD = dict(name="gauss16", N=1_048_576, n=16, seed=1, tc=512)
 RES_TOL = 1e-13
 
+# Roofline denominators, filled in by run_gpu_arm: the FP64 and FP32 FMA rates
+# measured on this GPU in this run (flop/s), and MEASURED_PEAKS.json's dense
+# BF16 tensor rate (flop/s) and copy bandwidth (B/s).
+PEAKS = {}
+
 
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
+
+
+def r4(x):
+    """A number rounded to 4 significant digits (keeps the JSON line short)."""
+    return float("%.4g" % x) if isinstance(x, float) else x
+
+
+def roofline(seconds, fp64=0.0, fp32=0.0, bf16=0.0, hbm=0.0):
+    """Roofline of one step from its ALGORITHMIC work: FP64 / FP32 / BF16 flops
+    and HBM bytes.  Per unit, frac = (work / step time) / measured peak; the
+    bound is the unit whose work takes longest at its peak, and the top-level
+    frac is that lower bound on the step time divided by the step time."""
+    units = {"fp64": (fp64, "TFLOP/s", 1e12), "fp32": (fp32, "TFLOP/s", 1e12), "bf16": (bf16, "TFLOP/s", 1e12),
+             "hbm": (hbm, "GB/s", 1e9)}
+    fracs = {}
+    for u, (work, _, _) in units.items():
+        if work > 0 and PEAKS.get(u):
+            fracs[u] = work / seconds / PEAKS[u]
+    bound = max(fracs, key=fracs.get)
+    work, unit, scale = units[bound]
+    return {"bound": bound, "achieved": r4(work / seconds / scale), "peak": r4(PEAKS[bound] / scale), "unit": unit,
+            "frac": r4(fracs[bound]), "fracs": {u: r4(f) for u, f in fracs.items()}}
+
+
+def fp64_flops(n, sweeps_total, matrices):
+    """24 n^3 + 20 s n^3 per matrix (Hessenberg 40/3 n^3, Q 16/3 n^3, back
+    substitution and back transformation 16/3 n^3, QR sweeps 20 n^2 per sweep of
+    the matrix), summed: sweeps_total = QR sweeps over all `matrices`."""
+    return 24.0 * n ** 3 * matrices + 20.0 * n * n * sweeps_total
+
+
+def hbm_bytes(n, matrices):
+    """Read A, write V and the eigenvalues: 32 n^2 + 16 n bytes per matrix."""
+    return (32.0 * n * n + 16.0 * n) * matrices
 
 
 # ----------------------------------------------------------------------------
@@ -248,7 +296,8 @@ def device_residual_check(dAr, dAi, dEr, dEi, dVr, dVi, n, tc, chunk=1 << 17):
 
 def measure_form(name, n, N, seed, tc, precision, warmup, steps):
     """Device-resident eigensolves/s of one form on one seeded Gaussian batch,
-    verified on the device afterwards (every residual)."""
+    verified on the device afterwards (every residual).  Returns the compact
+    entry of the JSON line and the detail record (stderr)."""
     import torch
     import ves
     import workloads
@@ -261,11 +310,12 @@ def measure_form(name, n, N, seed, tc, precision, warmup, steps):
     dVr, dVi = torch.empty_like(dAr), torch.empty_like(dAi)
     st = torch.zeros(N, dtype=torch.int32, device="cuda")
     sw = torch.zeros(N, dtype=torch.int32, device="cuda")
+    wc = torch.zeros(ves.VES_WORK_COUNTS, dtype=torch.int64, device="cuda")
     opt = ves.default_options(precision=precision)
     wsp = ves.Workspace(n, bc, tc, opt)
     stream = torch.cuda.current_stream()
-    run = lambda **kw: ves.eigensolve(n, bc, tc, dAr, dAi, dEr, dEi, dVr, dVi, options=opt, workspace=wsp,  # noqa: E731
-                                      stream=stream, **kw)
+    run = lambda o=opt, **kw: ves.eigensolve(n, bc, tc, dAr, dAi, dEr, dEi, dVr, dVi, options=o,  # noqa: E731
+                                             workspace=wsp, stream=stream, **kw)
     for _ in range(warmup):
         run()
     torch.cuda.synchronize()
@@ -276,21 +326,38 @@ def measure_form(name, n, N, seed, tc, precision, warmup, steps):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
-    run(status=st, sweeps=sw)
+    # the work of the step (results are deterministic: the same as every timed step)
+    run(ves.default_options(precision=precision, work_counts=wc), status=st, sweeps=sw)
     torch.cuda.synchronize()
     ver = device_residual_check(dAr, dAi, dEr, dEi, dVr, dVi, n, tc)
-    fb = int(((st & 8) != 0).sum())
+    fbm = (st & 8) != 0
+    fb = int(fbm.sum())
     other = int(((st & ~8) != 0).sum())
-    out = {"form": name, "n": n, "n_matrices": N, "seed": seed, "value": N / (ms * 1e-3), "unit": "eigensolves/s",
-           "ms_per_step": ms, "steps": steps, "warmup": warmup, "sweeps_per_eigenvalue": float(sw.double().mean()) / n,
-           "max_residual": ver["max_residual"], "median_residual": ver["median_residual"],
-           "nonfinite": ver["nonfinite"], "status_other": other,
-           "passed": ver["max_residual"] <= RES_TOL and ver["nonfinite"] == 0 and other == 0}
+    swd = sw.double()
+    res64, corr32, resff, _ = (int(x) for x in wc.tolist())
     if precision:
-        out["fp64_fallback_matrices"] = fb
+        # FP32: the reference path on the matrices that stayed in FP32, the Newton
+        # corrections (Z^H r 8n^2, bordered back substitution 4n^2, Z dx 8n^2) and
+        # the first residuals (8n^2, in float-float on the FP32 pipe); FP64: the
+        # accepting residuals (8n^2 + 16n with the norms) and the fallback solves
+        f32 = fp64_flops(n, float(swd[~fbm].sum()), N - fb) + corr32 * 20.0 * n * n + resff * 8.0 * n * n
+        f64 = fp64_flops(n, float(swd[fbm].sum()), fb) + res64 * (8.0 * n * n + 16.0 * n)
+    else:
+        f32, f64 = 0.0, fp64_flops(n, float(swd.sum()), N)
+    rl = roofline(ms * 1e-3, fp64=f64, fp32=f32, hbm=hbm_bytes(n, N))
+    passed = ver["max_residual"] <= RES_TOL and ver["nonfinite"] == 0 and other == 0
+    out = {"form": name, "n": n, "N": N, "value": r4(N / (ms * 1e-3)), "ms": r4(ms), "roofline": rl,
+           "s": r4(float(swd.mean()) / n), "max_res": r4(ver["max_residual"]), "passed": passed}
+    detail = {"form": name, "n": n, "n_matrices": N, "seed": seed, "steps": steps, "warmup": warmup,
+              "median_residual": ver["median_residual"], "nonfinite": ver["nonfinite"], "status_other": other,
+              "flops_fp64": f64, "flops_fp32": f32}
+    if precision:
+        out["fb"] = fb
+        detail.update(fp64_fallback_matrices=fb, fp64_residuals=res64, fp32_corrections=corr32,
+                      ff_residuals=resff, fp64_residuals_per_pair=res64 / max(1, (N - fb) * n))
     del dAr, dAi, dEr, dEi, dVr, dVi, wsp
     torch.cuda.empty_cache()
-    return out
+    return out, detail
 
 
 def _mat(re, im, n, tc):
@@ -383,29 +450,44 @@ def measure_learned(n, N, train_count, steps, tc=512):
     ms_plain = timed(plain)
     ms_learned = timed(learned)
     plain(sweeps=sw0)
+    wc = torch.zeros(ves.VES_WORK_COUNTS, dtype=torch.int64, device="cuda")
+    lopt.work_counts = wc.data_ptr()
     learned(status=st, sweeps=sw, fallbacks=fb)
     torch.cuda.synchronize()
+    lopt.work_counts = None
     ver = device_residual_check(rA, iA, rE, iE, rV, iV, n, tc)
     A = _mat(rA, iA, n, tc)
     err = eig_distance(_vec(rE, iE, n, tc), _vec(rE0, iE0, n, tc), A)
     pred_err = (_vec(rS, iS, n, tc)[:, :, None] - _vec(rE0, iE0, n, tc)[:, None, :]).abs().amin(dim=2)
     nA = torch.linalg.matrix_norm(A)
     other = int(((st & ~4) != 0).sum())
-    out = {"form": "learned shift", "n": n, "n_matrices": N, "family": "A0 + p1 A1 + p2 A2 + p3 A3, p ~ U[-1,1]^3",
-           "value": N / (ms_learned * 1e-3), "unit": "eigensolves/s", "ms_per_step": ms_learned,
-           "plain_fp64_value": N / (ms_plain * 1e-3), "speedup_vs_plain": ms_plain / ms_learned,
-           "sweeps_per_eigenvalue": float(sw.double().mean()) / n,
-           "plain_sweeps_per_eigenvalue": float(sw0.double().mean()) / n,
-           "fallback_per_eigenvalue": float(fb.double().mean()) / n,
-           "prediction_error_median_rel": float((pred_err / nA[:, None]).median()),
-           "train": {"matrices": train_count, "epochs": epochs, "seconds": train_s, "loss_first": losses[0],
-                     "loss_last": losses[-1], "network": cfg["net"]},
-           "shift_polish": cfg["polish"], "shift_gate": cfg["gate"],
-           "max_residual": ver["max_residual"], "nonfinite": ver["nonfinite"], "max_eig_err_rel": err,
-           "passed": ver["max_residual"] <= RES_TOL and ver["nonfinite"] == 0 and err <= 1e-12 and other == 0}
+    # work of one step: the shift-seeded FP64 solve (its own sweeps); on the FP32
+    # pipe the polish (Hessenberg reduction 40/3 n^3 in the pre-pass for n <= 32,
+    # 8 n^2 per Newton step on det(H - sI), device-counted) and the network's FP32
+    # output layer (2 * hidden * 2n); on the tensor cores the BF16 hidden layers
+    # (2 * (features * hidden + (layers - 1) * hidden^2) per matrix)
+    polish_steps = int(wc[ves.VES_WORK_POLISH])
+    h, L, F = cfg["net"]["hidden"], cfg["net"]["layers"], cfg["net"]["fourier"]
+    kin = 3 + 2 * 3 * F + 2 * n
+    f64 = fp64_flops(n, float(sw.double().sum()), N)
+    f32 = polish_steps * 8.0 * n * n + (N * 40.0 / 3.0 * n ** 3 if n <= 32 else 0.0) + N * 2.0 * h * 2 * n
+    fbf16 = N * 2.0 * (kin * h + (L - 1) * h * h)
+    rl = roofline(ms_learned * 1e-3, fp64=f64, fp32=f32, bf16=fbf16, hbm=hbm_bytes(n, N))
+    passed = ver["max_residual"] <= RES_TOL and ver["nonfinite"] == 0 and err <= 1e-12 and other == 0
+    out = {"form": "learned shift", "n": n, "N": N, "value": r4(N / (ms_learned * 1e-3)), "ms": r4(ms_learned),
+           "vs_plain": r4(ms_plain / ms_learned), "roofline": rl, "s": r4(float(sw.double().mean()) / n),
+           "s_plain": r4(float(sw0.double().mean()) / n), "max_res": r4(ver["max_residual"]), "passed": passed}
+    detail = {"form": "learned shift", "n": n, "n_matrices": N, "family": "A0 + p1 A1 + p2 A2 + p3 A3, p ~ U[-1,1]^3",
+              "plain_fp64_value": N / (ms_plain * 1e-3), "fallback_per_eigenvalue": float(fb.double().mean()) / n,
+              "prediction_error_median_rel": float((pred_err / nA[:, None]).median()),
+              "train": {"matrices": train_count, "epochs": epochs, "seconds": train_s, "loss_first": losses[0],
+                        "loss_last": losses[-1], "network": cfg["net"]},
+              "shift_polish": cfg["polish"], "shift_gate": cfg["gate"], "polish_newton_steps": polish_steps,
+              "flops_fp64": f64, "flops_fp32": f32, "flops_bf16": fbf16,
+              "nonfinite": ver["nonfinite"], "max_eig_err_rel": err}
     del net, rA, iA, rV, iV, ws, lws, pws, A
     torch.cuda.empty_cache()
-    return out
+    return out, detail
 
 
 def measure_varsize(count, steps, seed=2, max_dim=64):
@@ -478,18 +560,18 @@ def measure_varsize(count, steps, seed=2, max_dim=64):
             ves.eigensolve(n, 1, k, rs, is_, eb, eb2, vb, vb2, workspace=w, stream=stream)
 
     ms_per_order = timed(per_order, max(1, steps // 2))
-    out = {"form": "mixed-size batch", "n_matrices": count, "orders": "uniform in [4, %d]" % max_dim,
-           "families": "Gaussian / non-normal (cond(V)=1e4) / clustered (4 centres, radius 1e-6)",
-           "value": count / (ms * 1e-3), "unit": "eigensolves/s", "ms_per_step": ms,
-           "api": "ves_eigensolve_varsize captured in a CUDA graph, replayed",
-           "algorithmic_tflops": flops / (ms * 1e-3) / 1e12,
-           "sweeps_per_eigenvalue": float(sw.double().sum()) / float(nd.sum()),
-           "per_order_launches_value": count / (ms_per_order * 1e-3),
-           "speedup_vs_per_order_launches": ms_per_order / ms, "max_residual": worst, "status_nonzero": bad,
+    rl = roofline(ms * 1e-3, fp64=flops, hbm=float((32.0 * nd * nd + 16.0 * nd).sum()))
+    out = {"form": "mixed-size batch", "n": "4..%d" % max_dim, "N": count, "value": r4(count / (ms * 1e-3)),
+           "ms": r4(ms), "vs_per_order": r4(ms_per_order / ms), "roofline": rl,
+           "s": r4(float(sw.double().sum()) / float(nd.sum())), "max_res": r4(worst),
            "passed": worst <= RES_TOL and bad == 0}
+    detail = {"form": "mixed-size batch", "n_matrices": count, "orders": "uniform in [4, %d]" % max_dim,
+              "families": "Gaussian / non-normal (cond(V)=1e4) / clustered (4 centres, radius 1e-6)",
+              "api": "ves_eigensolve_varsize captured in a CUDA graph, replayed", "flops_fp64": flops,
+              "per_order_launches_value": count / (ms_per_order * 1e-3), "status_nonzero": bad}
     del g, bufs, per_n, re, im, vr, vi, er, ei, w
     torch.cuda.empty_cache()
-    return out
+    return out, detail
 
 
 def flops_per_matrix(n, s):
@@ -526,6 +608,13 @@ def run_gpu_arm(args, d):
                        sweeps=sw if with_stats else None, options=opt, workspace=wsp, stream=stream)
 
     peak_fp64 = ves.fp64_fma_rate(stream)
+    peaks_file = {}
+    try:
+        peaks_file = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    PEAKS.update(fp64=peak_fp64, fp32=ves.fp32_fma_rate(stream),
+                 bf16=peaks_file.get("bf16_tflops", 1900.0) * 1e12, hbm=peaks_file.get("hbm_gbs", 6800.0) * 1e9)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -555,13 +644,8 @@ def run_gpu_arm(args, d):
 
     launch_s = ms * 1e-3 / args.steps
     achieved = N * flops_per_matrix(n, s_mean) / launch_s
-    hbm_bytes = N * (32.0 * n * n + 16.0 * n)
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    hbm_b = hbm_bytes(n, N)
+    hbm_peak = PEAKS["hbm"] / 1e9
     traffic = read_traffic()
 
     # e2e through the drop-in with pinned host buffers
@@ -580,28 +664,37 @@ def run_gpu_arm(args, d):
                "sample": "first %d matrices of the batch, %d repetitions (%.1f s), OpenMP over %d threads"
                          % (sample, reps, tot, cores)}
 
-    forms = []
+    # The other forms, each on its own batch.  The JSON line carries a compact
+    # entry per form (value, speed-up, roofline, residual, verdict); the full
+    # record of each goes to stderr.
+    forms, details = [], []
     want = set(args.forms.split(",")) if args.forms else {"mixed16", "n32", "learned", "learned24", "varsize"}
+
+    def add(res):
+        forms.append(res[0])
+        details.append(res[1])
+        log("[bench] form detail: " + json.dumps(res[1]))
+
     if d.world == 1 and not args.no_forms:
         if "mixed16" in want:
-            forms.append(dict(measure_form("FP32+refine", n, N, w["seed"], tc, 1, 2, args.steps),
-                              speedup_vs_plain=None))
-            forms[-1]["speedup_vs_plain"] = forms[-1]["value"] / value
+            log("[bench] FP32+refine form, n=16")
+            add(measure_form("FP32+refine", n, N, w["seed"], tc, 1, 2, args.steps))
+            forms[-1]["vs_plain"] = r4(forms[-1]["value"] / value)
         if "n32" in want:
-            p32 = measure_form("plain FP64", 32, 262_144, 3, 512, 0, 1, 2)
-            m32 = measure_form("FP32+refine", 32, 262_144, 3, 512, 1, 1, 2)
-            m32["speedup_vs_plain"] = m32["value"] / p32["value"]
-            forms += [p32, m32]
+            log("[bench] plain FP64 and FP32+refine, n=32")
+            add(measure_form("plain FP64", 32, 262_144, 3, 512, 0, 1, 2))
+            add(measure_form("FP32+refine", 32, 262_144, 3, 512, 1, 1, 2))
+            forms[-1]["vs_plain"] = r4(forms[-1]["value"] / forms[-2]["value"])
         if "learned" in want:
             for ln in (16, 32):
                 log("[bench] learned-shift form, n=%d" % ln)
-                forms.append(measure_learned(ln, 262_144, 200_000, 2))
+                add(measure_learned(ln, 262_144, 200_000, 2))
         if "learned24" in want:
             log("[bench] learned-shift form, 1,048,576 x 24x24")
-            forms.append(measure_learned(24, 1 << 20, 200_000, 2))
+            add(measure_learned(24, 1 << 20, 200_000, 2))
         if "varsize" in want:
             log("[bench] mixed-size form")
-            forms.append(measure_varsize(500_000, 2))
+            add(measure_varsize(500_000, 2))
 
     d.done()
     if d.rank != 0:
@@ -620,9 +713,12 @@ def run_gpu_arm(args, d):
                      "peak_source": "FP64 FMA rate measured in this run (ves_fp64_fma_rate); "
                                     "MEASURED_PEAKS.json has no FP64 figure",
                      "flops_per_matrix": flops_per_matrix(n, s_mean),
-                     "hbm": {"achieved_gbs": hbm_bytes / launch_s / 1e9, "peak_gbs": hbm_peak,
-                             "frac": hbm_bytes / launch_s / 1e9 / hbm_peak, "bytes_per_matrix": 32 * n * n + 16 * n,
+                     "hbm": {"achieved_gbs": hbm_b / launch_s / 1e9, "peak_gbs": hbm_peak,
+                             "frac": hbm_b / launch_s / 1e9 / hbm_peak, "bytes_per_matrix": 32 * n * n + 16 * n,
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}},
+        "peaks": {"fp64_tflops": r4(PEAKS["fp64"] / 1e12), "fp32_tflops": r4(PEAKS["fp32"] / 1e12),
+                  "bf16_tflops": r4(PEAKS["bf16"] / 1e12), "hbm_gbs": r4(PEAKS["hbm"] / 1e9),
+                  "source": "FP64/FP32: FMA-rate probes run in this process; BF16, HBM: MEASURED_PEAKS.json"},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": ck,
@@ -630,9 +726,14 @@ def run_gpu_arm(args, d):
         "verify": dict(ver, status_nonzero=bad_status, passed=ok),
         "forms": forms,
     }
-    print(json.dumps(out), flush=True)
+    for f in forms:
+        rl = f["roofline"]
+        log("[bench] %-16s n=%-7s %12.6g eigensolves/s  %-16s roofline %s %.3f of measured  max residual %.2e%s"
+            % (f["form"], f["n"], f["value"], ("x%.3g" % f.get("vs_plain", f.get("vs_per_order", 0))),
+               rl["bound"], rl["frac"], f["max_res"], "" if f["passed"] else "  FAILED"))
+    print(json.dumps(out, separators=(",", ":")), flush=True)
     if not ok or not all(f["passed"] for f in forms):
-        log("[bench] VERIFICATION FAILED: %s" % json.dumps([out["verify"]] + forms))
+        log("[bench] VERIFICATION FAILED: %s" % json.dumps([out["verify"]] + details))
         sys.exit(1)
 
 

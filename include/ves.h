@@ -136,7 +136,19 @@ typedef struct ves_options {
                         * Hessenberg matrix) that refine each prediction before the QR; a prediction that does
                         * not converge or lands on an eigenvalue already seeded is dropped; for dim <= 32 this
                         * runs as a warp-per-matrix pre-pass; 0 (default) = none */
+    unsigned long long *work_counts; /* nullable DEVICE array of VES_WORK_COUNTS counters that the call ADDS to
+                        * (zero them first; stream-ordered like the outputs): the work of the data-dependent
+                        * stages, for flop accounting.  Default NULL. */
 } ves_options;
+
+/* Indices into ves_options.work_counts. */
+enum {
+    VES_WORK_RES64 = 0,   /* FP32_REFINE: FP64 residuals r = A v - lambda v (one per pair and Newton step) */
+    VES_WORK_CORR32 = 1,  /* FP32_REFINE: FP32 Newton corrections through the Schur form */
+    VES_WORK_RESFF = 2,   /* FP32_REFINE: first residuals in float-float (one per refined pair) */
+    VES_WORK_POLISH = 3,  /* ves_eigensolve_shifts: FP32 Newton steps on det(H - sI), over all predictions */
+    VES_WORK_COUNTS = 4
+};
 
 void ves_default_options(ves_options *opt);
 
@@ -165,7 +177,16 @@ size_t ves_eigensolve_workspace_size(int dim, int block_cnt, int thread_cnt, con
  * hold ves_eigensolve_workspace_size() bytes, 256-byte aligned.  Asynchronous
  * on `stream`; for large batches the FP32 + refinement form runs on two
  * library streams forked from `stream` by an event and joined back into it
- * (VES_MIXED_OVERLAP=0 in the environment keeps everything on `stream`). */
+ * (VES_MIXED_OVERLAP=0 in the environment keeps everything on `stream`).
+ * The two library streams are shared by all callers on a device: concurrent
+ * FP32 + refinement calls from several host threads are correct (each with
+ * its own workspace) but their overlapped stages run one call after the
+ * other.  While `stream` is being captured into a CUDA graph the call stays
+ * on `stream` (the two stages in sequence), so no library stream joins the
+ * capture.  An FP32 + refinement pair is accepted only if no other eigenvalue
+ * of its matrix lies within 16 refine_tol ||A||_F of it (two Newton runs that
+ * converged to one eigenvalue would otherwise hide another); such a matrix is
+ * solved in FP64 instead. */
 int ves_eigensolve(int dim, int block_cnt, int thread_cnt,
                    const double *rA, const double *iA, double *rE, double *iE, double *rV, double *iV,
                    double *rT, double *iT, int *status, int *sweeps,
@@ -308,6 +329,9 @@ int ves_backsubstitution(int dim, int block_cnt, int thread_cnt, const double *r
  * few milliseconds of dependent-FMA chains on all SMs; synchronous.  No
  * counterpart in the reference. */
 int ves_fp64_fma_rate(double *flops_per_s, void *stream);
+/* The same for FP32 FMAs: the roofline denominator of the FP32 stages of the
+ * FP32 + refinement form and of the learned-shift polish. */
+int ves_fp32_fma_rate(double *flops_per_s, void *stream);
 
 /* Allocation-free variant of ves_eigensolve (FP64, reference eigenvector
  * scaling, no Schur-form or sweep output).  No counterpart in the reference.
@@ -322,7 +346,10 @@ int ves_fp64_fma_rate(double *flops_per_s, void *stream);
  * larger dims return VES_ERR_ARG with a message in ves_last_error().
  * The first call on each device looks up the array's device address
  * (cudaGetSymbolAddress) with that device current: make that first call
- * before any stream capture.  All calls on a device share the array, so calls
+ * before any stream capture.  cudaDeviceReset() ends the context that holds
+ * the array, and the address looked up before it is then stale: do not call
+ * this entry point on a device after resetting it in the same process.
+ * All calls on a device share the array, so calls
  * that overlap on the GPU race and must be serialised by the caller.
  * Asynchronous on `stream`. */
 #define VES_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)

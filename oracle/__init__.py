@@ -62,9 +62,14 @@ _cache = {}
 def build(ref=True):
     """Compile the restatement (and the reference harness when its sources exist)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    if ref and os.path.exists(os.path.join(os.environ.get("VES_REFERENCE_DIR", "/root/reference"), "utils.cpp")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref",
-                        "REF=" + os.environ.get("VES_REFERENCE_DIR", "/root/reference")], check=True)
+    if ref and os.path.exists(os.path.join(reference_dir(), "utils.cpp")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + reference_dir()], check=True)
+
+
+def reference_dir():
+    """The reference checkout: $VES_REFERENCE_DIR, else a directory named
+    "reference" beside the repository (absent on machines without it)."""
+    return os.environ.get("VES_REFERENCE_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 
 def _load(path, sigs):

@@ -227,3 +227,118 @@ def test_mixed_overlap_equals_serial(n, N, monkeypatch):
     for a, b in zip(*outs):
         np.testing.assert_array_equal(a, b)
     assert ((outs[0][4] & ~ves.VES_STATUS_REFINE_FALLBACK) == 0).all()
+
+
+def _unitary(rng, n):
+    q, r = np.linalg.qr(cgauss(rng, (n, n)))
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def test_mixed_close_clusters_no_duplicate_eigenvalues():
+    """Normal matrices whose eigenvalues come in clusters 1e-9 ||A||_F wide:
+    far below FP32 resolution, so Newton from the FP32 Schur form can bring
+    two pairs to one eigenvalue.  Every true eigenvalue must still be found to
+    1e-12 ||A||_F (a duplicate would leave one ~1e-9 away), either by the
+    refinement or by the FP64 solve the distinctness check hands it to."""
+    rng = np.random.default_rng(23)
+    n, N, tc = 16, 256, 32
+    A = np.empty((N, n, n), complex)
+    lam = np.empty((N, n), complex)
+    for k in range(N):
+        centres = cgauss(rng, 4)
+        off = cgauss(rng, n) / np.sqrt(2)
+        lam[k] = np.repeat(centres, n // 4) + 1e-9 * np.linalg.norm(centres) * off
+        U = _unitary(rng, n)
+        A[k] = U @ np.diag(lam[k]) @ U.conj().T
+    out = run_fused(A, tc, precision=MIX)
+    nA = np.linalg.norm(A, axis=(1, 2))
+    _, err, _ = match_eigs(out["E"], lam)
+    assert (err / nA).max() <= 1e-12, (err / nA).max()
+    assert residuals(A, out["E"], out["V"]).max() <= 1e-13
+    assert (out["status"] & ~ves.VES_STATUS_REFINE_FALLBACK == 0).all()
+
+
+def test_mixed_work_counters():
+    """work_counts: one float-float residual per refined pair, at least one
+    FP64 residual and one FP32 correction per pair; nothing counted without
+    the option."""
+    import torch
+    rng = np.random.default_rng(31)
+    n, N, tc = 12, 512, 32
+    A = cgauss(rng, (N, n, n))
+    wc = torch.zeros(ves.VES_WORK_COUNTS, dtype=torch.int64, device="cuda")
+    out = run_fused(A, tc, precision=MIX, work_counts=wc)
+    fb = int(((out["status"] & ves.VES_STATUS_REFINE_FALLBACK) != 0).sum())
+    res64, corr, ff, polish = (int(x) for x in wc.cpu())
+    pairs = (N - fb) * n
+    assert ff == pairs
+    assert pairs <= res64 <= 9 * pairs and pairs <= corr <= 9 * pairs
+    assert polish == 0
+
+
+def test_mixed_concurrent_callers():
+    """Two host threads, each with its own stream and workspace, run the
+    FP32+refine form at once (large enough for the overlapped two-stream
+    path, whose library streams they share): each gets the result of a call
+    made alone, bit for bit."""
+    import threading
+
+    import torch
+    n, N, tc = 8, 65536, 512
+    batches = [workloads.gaussian_soa(N, n, s, tc) for s in (41, 42)]
+    opt = ves.default_options(precision=MIX)
+
+    def solve(b, stream, out, idx):
+        with torch.cuda.stream(stream):
+            dA = [torch.from_numpy(x).cuda() for x in b]
+            dE = [torch.empty(N * n, dtype=torch.float64, device="cuda") for _ in range(2)]
+            dV = [torch.empty_like(dA[0]) for _ in range(2)]
+            ws = ves.Workspace(n, N // tc, tc, opt)
+            for _ in range(3):
+                ves.eigensolve(n, N // tc, tc, dA[0], dA[1], dE[0], dE[1], dV[0], dV[1], options=opt, workspace=ws,
+                               stream=stream)
+            stream.synchronize()
+            out[idx] = [t.cpu().numpy() for t in dE + dV]
+
+    alone = [None, None]
+    for i, b in enumerate(batches):
+        solve(b, torch.cuda.Stream(), alone, i)
+    together = [None, None]
+    ths = [threading.Thread(target=solve, args=(b, torch.cuda.Stream(), together, i)) for i, b in enumerate(batches)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    for i in range(2):
+        for a, b in zip(alone[i], together[i]):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_mixed_graph_capture():
+    """A FP32+refine call captured in a CUDA graph (it stays on the capturing
+    stream instead of forking the shared library streams) replays to the
+    result of a direct call, bit for bit."""
+    import torch
+    n, N, tc = 8, 65536, 512
+    rA, iA = workloads.gaussian_soa(N, n, 43, tc)
+    dA = [torch.from_numpy(x).cuda() for x in (rA, iA)]
+    opt = ves.default_options(precision=MIX)
+    ws = ves.Workspace(n, N // tc, tc, opt)
+    outs = []
+    for captured in (False, True):
+        dE = [torch.zeros(N * n, dtype=torch.float64, device="cuda") for _ in range(2)]
+        dV = [torch.zeros_like(dA[0]) for _ in range(2)]
+        st = torch.full((N,), -1, dtype=torch.int32, device="cuda")
+        call = lambda: ves.eigensolve(n, N // tc, tc, dA[0], dA[1], dE[0], dE[1], dV[0], dV[1], status=st,  # noqa
+                                      options=opt, workspace=ws, stream=torch.cuda.current_stream())
+        if captured:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                call()
+            g.replay()
+        else:
+            call()
+        torch.cuda.synchronize()
+        outs.append([t.cpu().numpy() for t in dE + dV + [st]])
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a, b)

@@ -19,7 +19,8 @@ INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(HERE, "libves.so")
 OBJDIR = os.path.join(HERE, "_build")
 
-SOURCES = ["ves_kernels.cu", "ves_mixed.cu", "ves_extras.cu", "ves_varsize.cu", "ves_noalloc.cu", "ves_shiftnet.cu", "ves_api.cu"]
+SOURCES = ["ves_kernels.cu", "ves_mixed.cu", "ves_extras.cu", "ves_varsize.cu", "ves_noalloc.cu", "ves_shiftnet.cu",
+           "ves_api.cu", "ves_dropin_cxx.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 EXTRA = {}  # per-source extra nvcc flags

@@ -448,42 +448,44 @@ namespace ves {
 void set_error_message(const char *msg) { t_last_error = msg ? msg : ""; }
 }  // namespace ves
 
-extern "C" {
+namespace ves {
 
-// ------------------------------- drop-in ----------------------------------
-void eigensolver(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rE, double *iE, double *rV,
+// The drop-in bodies behind the C names below and the C++ names of
+// ves_dropin_cxx.cpp (the reference declares its host API with C++
+// linkage, utils.h:37-65; the Cython module binds utils.cpp the same way).
+void dropin_eigensolver(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rE, double *iE, double *rV,
                  double *iV)
 {
     dropin("eigensolver", [&] { return do_eigensolver(dim, block_cnt, thread_cnt, rA, iA, rE, iE, rV, iV); });
 }
 
-void hessenberg(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rQ, double *iQ)
+void dropin_hessenberg(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rQ, double *iQ)
 {
     dropin("hessenberg", [&] { return do_hessenberg(dim, block_cnt, thread_cnt, rA, iA, rQ, iQ); });
 }
 
-void call_zgehrd(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau)
+void dropin_call_zgehrd(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau)
 {
     dropin("call_zgehrd", [&] { return do_zgehrd(dim, block_cnt, thread_cnt, rA, iA, rtau, itau); });
 }
 
-void call_zunghr(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau)
+void dropin_call_zunghr(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau)
 {
     dropin("call_zunghr", [&] { return do_zunghr(dim, block_cnt, thread_cnt, rA, iA, rtau, itau); });
 }
 
-void call_zlahqr_new(int dim, int block_cnt, int thread_cnt, double *rE, double *iE, double *rM, double *iM, double *rS,
+void dropin_call_zlahqr_new(int dim, int block_cnt, int thread_cnt, double *rE, double *iE, double *rM, double *iM, double *rS,
                      double *iS)
 {
     dropin("call_zlahqr_new", [&] { return do_zlahqr(dim, block_cnt, thread_cnt, rE, iE, rM, iM, rS, iS); });
 }
 
-void call_ztrevc(int dim, int block_cnt, int thread_cnt, double *rT, double *iT, double *rR, double *iR)
+void dropin_call_ztrevc(int dim, int block_cnt, int thread_cnt, double *rT, double *iT, double *rR, double *iR)
 {
     dropin("call_ztrevc", [&] { return do_ztrevc(dim, block_cnt, thread_cnt, rT, iT, rR, iR); });
 }
 
-void call_zgemv(bool hermitian, int dim, int block_cnt, int thread_cnt, double *rM, double *iM, double *rx, double *ix,
+void dropin_call_zgemv(bool hermitian, int dim, int block_cnt, int thread_cnt, double *rM, double *iM, double *rx, double *ix,
                 double *ry, double *iy, double rbeta, double ibeta)
 {
     dropin("call_zgemv", [&] {
@@ -491,12 +493,12 @@ void call_zgemv(bool hermitian, int dim, int block_cnt, int thread_cnt, double *
     });
 }
 
-void call_backsubstitution(int dim, int block_cnt, int thread_cnt, double *rT, double *iT, double *rb, double *ib)
+void dropin_call_backsubstitution(int dim, int block_cnt, int thread_cnt, double *rT, double *iT, double *rb, double *ib)
 {
     dropin("call_backsubstitution", [&] { return do_backsubs(dim, block_cnt, thread_cnt, rT, iT, rb, ib); });
 }
 
-void repMatrixSoA(int dim, int block_cnt, int thread_cnt, double *matrix, double *out)
+void dropin_repMatrixSoA(int dim, int block_cnt, int thread_cnt, double *matrix, double *out)
 {
     const long long n2 = (long long)dim * dim;
     for (long long e = 0; e < n2; ++e)
@@ -504,14 +506,14 @@ void repMatrixSoA(int dim, int block_cnt, int thread_cnt, double *matrix, double
             for (long long t = 0; t < thread_cnt; ++t) out[b * thread_cnt * n2 + e * thread_cnt + t] = matrix[e];
 }
 
-void repVectorSoA(int dim, int block_cnt, int thread_cnt, double *vec, double *out)
+void dropin_repVectorSoA(int dim, int block_cnt, int thread_cnt, double *vec, double *out)
 {
     for (long long e = 0; e < dim; ++e)
         for (long long b = 0; b < block_cnt; ++b)
             for (long long t = 0; t < thread_cnt; ++t) out[b * thread_cnt * dim + e * thread_cnt + t] = vec[e];
 }
 
-void rearrangeMatrices(int dim, int block_cnt, int thread_cnt, double *in, double *out)
+void dropin_rearrangeMatrices(int dim, int block_cnt, int thread_cnt, double *in, double *out)
 {
     const long long n2 = (long long)dim * dim;
     for (long long b = 0; b < block_cnt; ++b)
@@ -520,13 +522,81 @@ void rearrangeMatrices(int dim, int block_cnt, int thread_cnt, double *in, doubl
                 out[b * thread_cnt * n2 + e * thread_cnt + t] = in[(b * thread_cnt + t) * n2 + e];
 }
 
-void arrangeMatricesAoS(int dim, int block_cnt, int thread_cnt, double *in, double *out)
+void dropin_arrangeMatricesAoS(int dim, int block_cnt, int thread_cnt, double *in, double *out)
 {
     const long long n2 = (long long)dim * dim;
     for (long long b = 0; b < block_cnt; ++b)
         for (long long t = 0; t < thread_cnt; ++t)
             for (long long e = 0; e < n2; ++e)
                 out[(b * thread_cnt + t) * n2 + e] = in[b * thread_cnt * n2 + e * thread_cnt + t];
+}
+
+}  // namespace ves
+
+extern "C" {
+
+// ------------------------------- drop-in ----------------------------------
+void eigensolver(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rE, double *iE,
+                 double *rV, double *iV)
+{
+    ves::dropin_eigensolver(dim, block_cnt, thread_cnt, rA, iA, rE, iE, rV, iV);
+}
+
+void hessenberg(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rQ, double *iQ)
+{
+    ves::dropin_hessenberg(dim, block_cnt, thread_cnt, rA, iA, rQ, iQ);
+}
+
+void call_zgehrd(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau)
+{
+    ves::dropin_call_zgehrd(dim, block_cnt, thread_cnt, rA, iA, rtau, itau);
+}
+
+void call_zunghr(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau)
+{
+    ves::dropin_call_zunghr(dim, block_cnt, thread_cnt, rA, iA, rtau, itau);
+}
+
+void call_zlahqr_new(int dim, int block_cnt, int thread_cnt, double *rE, double *iE, double *rM, double *iM,
+                     double *rS, double *iS)
+{
+    ves::dropin_call_zlahqr_new(dim, block_cnt, thread_cnt, rE, iE, rM, iM, rS, iS);
+}
+
+void call_ztrevc(int dim, int block_cnt, int thread_cnt, double *rT, double *iT, double *rR, double *iR)
+{
+    ves::dropin_call_ztrevc(dim, block_cnt, thread_cnt, rT, iT, rR, iR);
+}
+
+void call_zgemv(bool hermitian, int dim, int block_cnt, int thread_cnt, double *rM, double *iM, double *rx,
+                double *ix, double *ry, double *iy, double rbeta, double ibeta)
+{
+    ves::dropin_call_zgemv(hermitian, dim, block_cnt, thread_cnt, rM, iM, rx, ix, ry, iy, rbeta, ibeta);
+}
+
+void call_backsubstitution(int dim, int block_cnt, int thread_cnt, double *rT, double *iT, double *rb, double *ib)
+{
+    ves::dropin_call_backsubstitution(dim, block_cnt, thread_cnt, rT, iT, rb, ib);
+}
+
+void repMatrixSoA(int dim, int block_cnt, int thread_cnt, double *matrix, double *out)
+{
+    ves::dropin_repMatrixSoA(dim, block_cnt, thread_cnt, matrix, out);
+}
+
+void repVectorSoA(int dim, int block_cnt, int thread_cnt, double *vec, double *out)
+{
+    ves::dropin_repVectorSoA(dim, block_cnt, thread_cnt, vec, out);
+}
+
+void rearrangeMatrices(int dim, int block_cnt, int thread_cnt, double *in, double *out)
+{
+    ves::dropin_rearrangeMatrices(dim, block_cnt, thread_cnt, in, out);
+}
+
+void arrangeMatricesAoS(int dim, int block_cnt, int thread_cnt, double *in, double *out)
+{
+    ves::dropin_arrangeMatricesAoS(dim, block_cnt, thread_cnt, in, out);
 }
 
 // -------------------------------- native ----------------------------------
@@ -545,6 +615,7 @@ void ves_default_options(ves_options *opt)
     opt->shift_sweeps = 1;
     opt->shift_gate = 0.f;
     opt->shift_polish = 0;
+    opt->work_counts = nullptr;
 }
 
 size_t ves_eigensolve_workspace_size(int dim, int block_cnt, int thread_cnt, const ves_options *opt)
@@ -648,12 +719,18 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
     m.fb_list = list;
     m.fb_count = count;
     m.blocks_per_sm = o.blocks_per_sm;
+    m.work = o.work_counts;
     // The Schur stage of one chunk overlaps the refinement of the previous one on
     // two library streams (forked from and joined back into the caller's);
-    // VES_MIXED_OVERLAP=0 runs the two stages one after the other on the caller's stream.
+    // VES_MIXED_OVERLAP=0 runs the two stages one after the other on the caller's
+    // stream.  So does a call whose stream is being captured: the library streams
+    // are shared by every caller on the device, and forking them into one
+    // caller's capture would pull other callers' work into that graph.
     const char *ov = getenv("VES_MIXED_OVERLAP");
     cudaStream_t s_schur = nullptr, s_refine = nullptr;
-    if (!(ov && ov[0] == '0')) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (!cuda_ok(cudaStreamIsCapturing(st, &cap), "cudaStreamIsCapturing")) return VES_ERR_CUDA;
+    if (!(ov && ov[0] == '0') && cap == cudaStreamCaptureStatusNone) {
         s_schur = library_stream(0);
         s_refine = library_stream(1);
     }
@@ -814,7 +891,7 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *
         // n <= 32: polish in a warp-per-matrix FP32 pre-pass, the solve reads the result
         double *rP = reinterpret_cast<double *>(static_cast<char *>(ws) + plan.fused);
         double *iP = rP + (size_t)g.N * dim;
-        if (!cuda_ok(ves::launch_polish32(g, rA, iA, rS, iS, rP, iP, o.shift_polish, st), "shift polish launch"))
+        if (!cuda_ok(ves::launch_polish32(g, rA, iA, rS, iS, rP, iP, o.shift_polish, o.work_counts, st), "shift polish launch"))
             return VES_ERR_CUDA;
         a.rS = rP;
         a.iS = iP;
@@ -1034,6 +1111,13 @@ int ves_fp64_fma_rate(double *flops_per_s, void *stream)
     begin_call();
     if (!flops_per_s) { set_error("null pointer"); return VES_ERR_ARG; }
     return native(cuda_ok(ves::fp64_fma_rate(flops_per_s, (cudaStream_t)stream), "fp64 probe"));
+}
+
+int ves_fp32_fma_rate(double *flops_per_s, void *stream)
+{
+    begin_call();
+    if (!flops_per_s) { set_error("null pointer"); return VES_ERR_ARG; }
+    return native(cuda_ok(ves::fp32_fma_rate(flops_per_s, (cudaStream_t)stream), "fp32 probe"));
 }
 
 const char *ves_last_error(void) { return t_last_error.c_str(); }

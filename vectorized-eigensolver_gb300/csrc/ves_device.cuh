@@ -361,6 +361,56 @@ __device__ __forceinline__ int deflation_scan(const int I, const int L0, const M
     return K;
 }
 
+// The same deflation test evaluated in FP64 on an FP32 matrix (the FP32 +
+// refinement form keeps the deflation decision in FP64; the thresholds are
+// FP32's ulp and smlnum, the precision the QR runs in).  An FP32 screen
+// settles every subdiagonal that is clearly not negligible -- nearly all of
+// them: its sums and products round by a few 2^-24 relative, far inside the
+// 2^-20 margin, so the FP64 evaluation would decide the same.  Only the
+// others (the subdiagonals at or near deflation, and tst = 0) are tested in
+// FP64, so the decisions are those of a full FP64 evaluation.
+template <class MH>
+__device__ __forceinline__ int deflation_scan64(const int I, const int L0, const MH &H, const int n, const float ulp,
+                                                const float smlnum)
+{
+    const float margin = 1.0f + 0x1p-20f;
+    const double ulp64 = ulp, sml64 = smlnum;
+    int K;
+    for (K = I; K >= L0 + 1; --K) {
+        const cx<float> hkf = H.ld(K, K - 1), hkmf = H.ld(K - 1, K - 1), hkkf = H.ld(K, K);
+        const float tf = cabs1(hkmf) + cabs1(hkkf);
+        if (cabs1(hkf) > smlnum * margin && tf > 0.f && fabsf(hkf.r) > ulp * tf * margin) continue;
+        const cx<double> hk = mk((double)hkf.r, (double)hkf.i), hkm = mk((double)hkmf.r, (double)hkmf.i),
+                         hkk = mk((double)hkkf.r, (double)hkkf.i);
+        if (cabs1(hk) <= sml64) break;
+        double tst = cabs1(hkm) + cabs1(hkk);
+        if (tst == 0.0) {
+            if (K - 2 >= 1) tst += fabs((double)H.ld(K - 1, K - 2).r);
+            if (K + 1 <= n) tst += fabs((double)H.ld(K + 1, K).r);
+        }
+        if (fabs(hk.r) <= ulp64 * tst) {
+            const cx<float> hkuf = H.ld(K - 1, K);
+            double d2 = cabs1(hk), d3 = cabs1(mk((double)hkuf.r, (double)hkuf.i));
+            const double ab = fmax(d2, d3), ba = fmin(d2, d3);
+            d2 = cabs1(hkk);
+            d3 = cabs1(csub(hkm, hkk));
+            const double aa = fmax(d2, d3), bb = fmin(d2, d3);
+            const double s = aa + ab;
+            if (ba * (ab / s) <= fmax(sml64, ulp64 * (bb * (aa / s)))) break;
+        }
+    }
+    return K;
+}
+
+// deflation_scan, or for kDefl64 (FP32 data only) deflation_scan64
+template <class R, bool kDefl64, class MH>
+__device__ __forceinline__ int deflation_scan_sel(const int I, const int L0, const MH &H, const int n, const R ulp,
+                                                  const R smlnum)
+{
+    if constexpr (kDefl64) return deflation_scan64(I, L0, H, n, (float)ulp, (float)smlnum);
+    else return deflation_scan<R>(I, L0, H, n, ulp, smlnum);
+}
+
 // Shift for sweep number `its` on the active block L..I (reference :896-990).
 template <class R, class MH>
 __device__ __forceinline__ cx<R> qr_shift(const int I, const int L, const int its, const MH &H)
@@ -644,7 +694,8 @@ __device__ void polish_shifts_lane(const int n, const MatIlv<float> &Hf, const V
     }
 }
 
-template <class R, bool kSchur = true, class MH, class MZ, class SP = NoShiftPredictions>
+// kDefl64 (FP32 data only): the deflation test in FP64 (deflation_scan64).
+template <class R, bool kSchur = true, bool kDefl64 = false, class MH, class MZ, class SP = NoShiftPredictions>
 __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool valid, const int max_its,
                             int &nsweeps, int &status, SP *sp = nullptr)
 {
@@ -663,7 +714,7 @@ __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool va
             for (;;) {
                 if (I <= 1) { done = true; break; }
                 if (its > max_its) { status |= ST_ITCAP; --I; L = 1; its = 0; continue; }
-                L = deflation_scan<R>(I, L, H, n, ulp, smlnum);
+                L = deflation_scan_sel<R, kDefl64>(I, L, H, n, ulp, smlnum);
                 if (L > 1) H.st(L, L - 1, mk(R(0), R(0)));
                 if (L >= I) {
                     if (sp) sp->deflated(its);

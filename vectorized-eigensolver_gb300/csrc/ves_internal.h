@@ -63,6 +63,7 @@ struct MixedArgs {
     // matrices [m_begin, m_end) of the batch (a multiple of 32 where a chunk
     // ends inside the batch); launch_mixed sets the whole batch when m_end == 0
     long long m_begin, m_end;
+    unsigned long long *work;  // optional work counters (WORK_*)
 };
 
 size_t mixed_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blocks, int *out_threads);
@@ -105,7 +106,7 @@ cudaError_t launch_fused_fp64_blocks(const FusedArgs &a, int blocks, cudaStream_
 // Learned-shift polish pre-pass (n <= 32): predictions (rS, iS) refined by
 // Newton steps on the FP32 Hessenberg form, written to (rP, iP); NaN = dropped.
 cudaError_t launch_polish32(Geom g, const double *rA, const double *iA, const double *rS, const double *iS,
-                            double *rP, double *iP, int steps, cudaStream_t st);
+                            double *rP, double *iP, int steps, unsigned long long *work, cudaStream_t st);
 
 // Eigenvalues only (no Q, no Schur vectors), companion-matrix roots, and the
 // SoA <-> interleaved-complex transposes.
@@ -129,11 +130,30 @@ cudaError_t launch_varsize(long long count, int max_dim, const int *dims, const 
 cudaError_t launch_gemm_bf16(int M, int N, int K, const void *A, int lda, const void *Bt, int ldb, const float *bias,
                              int act, void *C, float *Cf, int ldc, int *err, cudaStream_t st);
 
+// The drop-in bodies (ves_api.cu) behind the C names of ves.h and the C++
+// names of the reference host API (ves_dropin_cxx.cpp).
+void dropin_eigensolver(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rE, double *iE, double *rV, double *iV);
+void dropin_hessenberg(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rQ, double *iQ);
+void dropin_call_zgehrd(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau);
+void dropin_call_zunghr(int dim, int block_cnt, int thread_cnt, double *rA, double *iA, double *rtau, double *itau);
+void dropin_call_zlahqr_new(int dim, int block_cnt, int thread_cnt, double *rE, double *iE, double *rM, double *iM, double *rS, double *iS);
+void dropin_call_ztrevc(int dim, int block_cnt, int thread_cnt, double *rT, double *iT, double *rR, double *iR);
+void dropin_call_zgemv(bool hermitian, int dim, int block_cnt, int thread_cnt, double *rM, double *iM, double *rx, double *ix, double *ry, double *iy, double rbeta, double ibeta);
+void dropin_call_backsubstitution(int dim, int block_cnt, int thread_cnt, double *rT, double *iT, double *rb, double *ib);
+void dropin_repMatrixSoA(int dim, int block_cnt, int thread_cnt, double *matrix, double *out);
+void dropin_repVectorSoA(int dim, int block_cnt, int thread_cnt, double *vec, double *out);
+void dropin_rearrangeMatrices(int dim, int block_cnt, int thread_cnt, double *in, double *out);
+void dropin_arrangeMatricesAoS(int dim, int block_cnt, int thread_cnt, double *in, double *out);
+
 // Record the calling thread's message for ves_last_error().
 void set_error_message(const char *msg);
 
-// Measured FP64 FMA throughput of this GPU (2 flops per FMA).
+// Measured FP64 / FP32 FMA throughput of this GPU (2 flops per FMA).
 cudaError_t fp64_fma_rate(double *flops_per_s, cudaStream_t st);
+cudaError_t fp32_fma_rate(double *flops_per_s, cudaStream_t st);
+
+// Work counters of ves_options.work_counts (device, accumulated with atomics).
+enum { WORK_RES64 = 0, WORK_CORR32 = 1, WORK_RESFF = 2, WORK_POLISH = 3 };
 
 // CUDA loads a kernel lazily, at its first launch, by default, so where a
 // kernel's code lands depends on what the process loaded before.  Kernels that

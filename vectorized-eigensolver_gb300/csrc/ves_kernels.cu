@@ -440,7 +440,7 @@ __host__ __device__ __forceinline__ size_t polish_warp_elems(int n)
 __global__ void __launch_bounds__(kPolishThreads) polish32_warp_kernel(const Geom g, const double *rA,
                                                                        const double *iA, const double *rS,
                                                                        const double *iS, double *rP, double *iP,
-                                                                       int steps)
+                                                                       int steps, unsigned long long *work)
 {
     extern __shared__ float2 psm[];
     const int n = g.n, tc = g.tc;
@@ -480,9 +480,11 @@ __global__ void __launch_bounds__(kPolishThreads) polish32_warp_kernel(const Geo
         const float tol = 1e-6f * scale, keep = 1e-3f * scale, dup = 1e-5f * scale;
         bool ok = lane < n && !nonfinite(s.r) && !nonfinite(s.i);
         float last = 3.0e38f;
+        int nsteps = 0;  // Newton steps this lane's prediction took (work counter)
         for (int it = 0; it < steps; ++it) {
             const bool act = ok && last > tol;
             if (!__any_sync(FULL, act)) break;
+            nsteps += act;
             xs[(n - 1) * 32 + lane] = make_float2(1.f, 0.f);
             dxs[(n - 1) * 32 + lane] = make_float2(0.f, 0.f);
             bool broke = false;
@@ -544,6 +546,10 @@ __global__ void __launch_bounds__(kPolishThreads) polish32_warp_kernel(const Geo
         if (lane < n) {
             rP[vo + (long long)lane * tc] = res.r;
             iP[vo + (long long)lane * tc] = res.i;
+        }
+        if (work) {
+            const int tot = __reduce_add_sync(FULL, nsteps);
+            if (lane == 0 && tot) atomicAdd(work + WORK_POLISH, (unsigned long long)tot);
         }
         __syncwarp();
     }
@@ -652,12 +658,14 @@ __global__ void backsubs_kernel(const Geom g, const double *rT, const double *iT
 }
 
 
-// FP64 FMA throughput probe: the roofline denominator for the FP64-bound
-// solver (a measured figure, as the HBM and tensor peaks are).  Eight
-// independent dependent-FMA chains per thread, 8 warps per SM.
-__global__ void fp64_fma_probe_kernel(double *out, int iters, double b, double c)
+// FMA throughput probes: the roofline denominators of the FP64-bound solver
+// and of the FP32 stages of the mixed-precision form (measured figures, as
+// the HBM and tensor peaks are).  Eight independent dependent-FMA chains per
+// thread.
+template <class R>
+__global__ void fma_probe_kernel(R *out, int iters, R b, R c)
 {
-    double a0 = threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+    R a0 = threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
     for (int i = 0; i < iters; ++i) {
         a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
         a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
@@ -719,7 +727,7 @@ cudaError_t launch_fused_fp64(const FusedArgs &a, cudaStream_t st)
 }
 
 cudaError_t launch_polish32(Geom g, const double *rA, const double *iA, const double *rS, const double *iS,
-                            double *rP, double *iP, int steps, cudaStream_t st)
+                            double *rP, double *iP, int steps, unsigned long long *work, cudaStream_t st)
 {
     if (g.N <= 0) return cudaSuccess;
     if (g.n > 32) return cudaErrorInvalidValue;
@@ -734,7 +742,7 @@ cudaError_t launch_polish32(Geom g, const double *rA, const double *iA, const do
     const long long need = (g.N + kPolishThreads / 32 - 1) / (kPolishThreads / 32);
     const long long blocks = std::max<long long>(1, std::min<long long>(need, (long long)sms * std::max(per_sm, 1)));
     polish32_warp_kernel<<<(unsigned)blocks, kPolishThreads, polish_smem_bytes(g.n), st>>>(g, rA, iA, rS, iS, rP,
-                                                                                         iP, steps);
+                                                                                         iP, steps, work);
     return cudaGetLastError();
 }
 
@@ -818,22 +826,25 @@ cudaError_t launch_backsubs(Geom g, const double *rT, const double *iT, double *
     return cudaGetLastError();
 }
 
-cudaError_t fp64_fma_rate(double *flops_per_s, cudaStream_t st)
+// threads per SM: 8 warps keep the FP64 pipe full; the FP32 pipe (about 58x
+// the FP64 rate) needs 32 warps of independent chains
+template <class R>
+cudaError_t fma_rate(double *flops_per_s, cudaStream_t st, int threads, int iters)
 {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int threads = 256, iters = 4096;
-    double *out = nullptr;
-    cudaError_t e = cudaMallocAsync(&out, (size_t)sms * threads * sizeof(double), st);
+    R *out = nullptr;
+    cudaError_t e = cudaMallocAsync(&out, (size_t)sms * threads * sizeof(R), st);
     if (e != cudaSuccess) return e;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    fp64_fma_probe_kernel<<<sms, threads, 0, st>>>(out, iters, 1.0000001, 1e-9);  // warm-up
+    const R b = R(1.0000001), c = R(1e-9);
+    fma_probe_kernel<R><<<sms, threads, 0, st>>>(out, iters, b, c);  // warm-up
     cudaEventRecord(e0, st);
     const int reps = 5;
-    for (int r = 0; r < reps; ++r) fp64_fma_probe_kernel<<<sms, threads, 0, st>>>(out, iters, 1.0000001, 1e-9);
+    for (int r = 0; r < reps; ++r) fma_probe_kernel<R><<<sms, threads, 0, st>>>(out, iters, b, c);
     cudaEventRecord(e1, st);
     e = cudaEventSynchronize(e1);
     float ms = 0.f;
@@ -845,6 +856,9 @@ cudaError_t fp64_fma_rate(double *flops_per_s, cudaStream_t st)
     *flops_per_s = 2.0 * 8.0 * iters * (double)sms * threads * reps / (ms * 1e-3);
     return e;
 }
+
+cudaError_t fp64_fma_rate(double *flops_per_s, cudaStream_t st) { return fma_rate<double>(flops_per_s, st, 256, 4096); }
+cudaError_t fp32_fma_rate(double *flops_per_s, cudaStream_t st) { return fma_rate<float>(flops_per_s, st, 1024, 16384); }
 
 void load_fused_kernels()
 {
@@ -859,7 +873,8 @@ void load_fused_kernels()
     load_kernel(ztrevc_kernel);
     load_kernel(zgemv_kernel);
     load_kernel(backsubs_kernel);
-    load_kernel(fp64_fma_probe_kernel);
+    load_kernel(fma_probe_kernel<double>);
+    load_kernel(fma_probe_kernel<float>);
 }
 
 }  // namespace ves

@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kSchurThreads) schur32_kernel(const MixedArgs 
             zunghr_lane<float>(n, T, Z, W);
             clear_below_subdiag_lane<float>(n, T);
         }
-        zlahqr_warp<float>(n, T, Z, valid && !fb, a.max_its, sweeps, status);
+        zlahqr_warp<float, true, true>(n, T, Z, valid && !fb, a.max_its, sweeps, status);
         if (status & ST_ITCAP) fb = true;
         if (valid) {
             if (!fb) trevc_x_lane<float>(n, T, pX);
@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
             int I = n, L = 1, its = 0;
             while (I > 1) {
                 if (its > a.max_its) { status |= ST_ITCAP; --I; L = 1; its = 0; continue; }
-                L = deflation_scan<float>(I, L, H, n, ulp, smlnum);
+                L = deflation_scan64(I, L, H, n, ulp, smlnum);
                 __syncwarp(gmask);
                 if (L > 1 && gl == 0) H.st(L, L - 1, mk(0.f, 0.f));
                 __syncwarp(gmask);
@@ -418,10 +418,13 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
     const float etol2 = (float)(16.0 * tol2);
     const float xkk = act ? X.ld(k, k).r : 1.f;
     bool fail = false;
+    int n_res64 = 0, n_corr = 0, n_ff = 0;  // work counters: FP64 / float-float residuals, FP32 corrections
     for (int step = 0; step <= a.max_steps; ++step) {
         if (!__any_sync(FULL, act)) break;
         if (!act) continue;
         bool certified = false;
+        n_res64 += step > 0;
+        n_ff += step == 0;
         if (step == 0) {
             // First residual in float-float on the FP32 pipe: v0 and lambda0 are
             // FP32 numbers and A = Ah + Al, so every product splits exactly into
@@ -462,6 +465,7 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
             certified = rn2 <= tol2 * (double)nA2 * vn2;
         }
         if (!certified && step == a.max_steps) { fail = true; act = false; continue; }
+        ++n_corr;
         // FP32 correction through the Schur form: r' = Z^H r kept in dx
         for (int i = 1; i <= n; ++i) {
             cx<float> s = mk(0.f, 0.f);
@@ -498,6 +502,15 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
         }
         lam = cadd(lam, up(dl));
     }
+    if (a.work) {  // all lanes of the warp are here (the loop exits uniformly)
+        const int r64 = __reduce_add_sync(FULL, n_res64), c32 = __reduce_add_sync(FULL, n_corr);
+        const int ff = __reduce_add_sync(FULL, n_ff);
+        if ((threadIdx.x & 31) == 0) {
+            if (r64) atomicAdd(a.work + WORK_RES64, (unsigned long long)r64);
+            if (c32) atomicAdd(a.work + WORK_CORR32, (unsigned long long)c32);
+            if (ff) atomicAdd(a.work + WORK_RESFF, (unsigned long long)ff);
+        }
+    }
     if (!valid || flags[m] != 0) return;
     if (fail) {
         to_fp64_list(a, flags, m);
@@ -518,6 +531,44 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
     }
     const MatSoA<double> Vo{a.rV + mo, a.iV + mo, tc, n};
     for (int i = 1; i <= n; ++i) Vo.st(i, k, cscal(v[i - 1], scale));
+}
+
+// Distinctness of the refined eigenvalues of each matrix.  Newton from two
+// FP32 starting points can land on the same eigenpair when the FP32 Schur
+// form does not resolve a cluster: both pairs pass their residual and
+// correction tests, and the output holds one eigenvalue twice and misses
+// another.  Every accepted eigenvalue lies within 4 tol ||A||_F of a true one,
+// so two that converged to one eigenvalue are within 8 tol ||A||_F of each
+// other: a matrix with two eigenvalues closer than 16 tol ||A||_F goes to the
+// FP64 solver (two distinct eigenvalues that close are also left to it).  One
+// thread per matrix; pairs are screened in FP32 first (the rounding of the
+// FP32 copies is at most 2^-24 of each magnitude), the rest decided in FP64.
+template <bool kPerMatrix>
+__global__ void __launch_bounds__(128) dupcheck_kernel(const MixedArgs a, const float2 *buf, int *flags)
+{
+    const int n = a.g.n, tc = a.g.tc;
+    const long long m = a.m_begin + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= a.m_end || flags[m] != 0 || n < 2) return;
+    const long long nn = (long long)n * n;
+    const float2 *pT = buf + (kPerMatrix ? m * mat_elems(n) : (m / 32) * group_elems(n) * 32 + (m % 32));
+    const float nA2 = pT[3 * (kPerMatrix ? 1 : 32) * nn].x;
+    const double thr = 16.0 * a.tol * sqrt((double)nA2);
+    const float thr_f = (float)thr;
+    const long long vo = soa_off_m(m, n, tc);
+    bool dup = false;
+    for (int k = 1; k < n && !dup; ++k) {
+        const double kr = a.rE[vo + (long long)k * tc], ki = a.iE[vo + (long long)k * tc];
+        const float fkr = (float)kr, fki = (float)ki;
+        for (int j = 0; j < k; ++j) {
+            const double jr = a.rE[vo + (long long)j * tc], ji = a.iE[vo + (long long)j * tc];
+            const float dr = fkr - (float)jr, di = fki - (float)ji;
+            const float slack = 1.2e-7f * (fabsf(fkr) + fabsf(fki) + fabsf((float)jr) + fabsf((float)ji));
+            if (fabsf(dr) + fabsf(di) > thr_f * 1.5f + slack) continue;  // certainly farther apart than thr
+            const double er = kr - jr, ei = ki - ji;
+            if (fma(er, er, ei * ei) <= thr * thr) { dup = true; break; }
+        }
+    }
+    if (dup) to_fp64_list(a, flags, m);
 }
 
 // default blocks (4 warps each) per SM of the lane Schur kernel; VES_MIXED_BLOCKS_PER_SM overrides
@@ -657,6 +708,18 @@ cudaError_t launch_refine(const MixedArgs &a, cudaStream_t st)
     return cudaGetLastError();
 }
 
+// distinctness check of the refined eigenvalues of matrices [a.m_begin, a.m_end)
+cudaError_t launch_dupcheck(const MixedArgs &a, cudaStream_t st)
+{
+    const MixedBufs b = mixed_bufs(a);
+    const unsigned blocks = (unsigned)((a.m_end - a.m_begin + 127) / 128);
+    if (schur_group(a.g.n))
+        dupcheck_kernel<true><<<blocks, 128, 0, st>>>(a, b.buf, b.flags);
+    else
+        dupcheck_kernel<false><<<blocks, 128, 0, st>>>(a, b.buf, b.flags);
+    return cudaGetLastError();
+}
+
 MixedArgs whole_batch(const MixedArgs &a)
 {
     MixedArgs w = a;
@@ -675,8 +738,9 @@ cudaError_t launch_mixed(const MixedArgs &a0, cudaStream_t st)
     if (a0.g.n > 64) return cudaErrorInvalidValue;  // the refinement keeps per-pair vectors of at most 64 entries
     const MixedArgs a = whole_batch(a0);
     cudaError_t e = launch_schur(a, a.blocks_per_sm, st);
-    if (e != cudaSuccess) return e;
-    return launch_refine(a, st);
+    if (e == cudaSuccess) e = launch_refine(a, st);
+    if (e == cudaSuccess) e = launch_dupcheck(a, st);
+    return e;
 }
 
 cudaError_t launch_mixed_overlap(const MixedArgs &a0, cudaStream_t st, cudaStream_t s_schur, cudaStream_t s_refine)
@@ -707,7 +771,13 @@ cudaError_t launch_mixed_overlap(const MixedArgs &a0, cudaStream_t st, cudaStrea
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join_s, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join_r, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventRecord(fork, st);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(s_schur, fork, 0);
+    if (e != cudaSuccess) {  // nothing was queued on the library streams
+        if (fork) cudaEventDestroy(fork);
+        if (join_s) cudaEventDestroy(join_s);
+        if (join_r) cudaEventDestroy(join_r);
+        return e;
+    }
+    e = cudaStreamWaitEvent(s_schur, fork, 0);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s_refine, fork, 0);
     for (long long c = 0; c < nch && e == cudaSuccess; ++c) {
         MixedArgs ch = a;
@@ -721,13 +791,21 @@ cudaError_t launch_mixed_overlap(const MixedArgs &a0, cudaStream_t st, cudaStrea
         if (e == cudaSuccess) e = launch_refine(ch, s_refine);
         if (done) cudaEventDestroy(done);  // released once the device has passed it
     }
-    if (e == cudaSuccess) e = cudaEventRecord(join_s, s_schur);
-    if (e == cudaSuccess) e = cudaEventRecord(join_r, s_refine);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, join_s, 0);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, join_r, 0);
-    if (fork) cudaEventDestroy(fork);
-    if (join_s) cudaEventDestroy(join_s);
-    if (join_r) cudaEventDestroy(join_r);
+    // Join the library streams back into the caller's stream even after a
+    // failed launch: work already queued on them writes the caller's outputs
+    // and workspace, and must be ordered before anything the caller does next.
+    // Where the join itself cannot be recorded, wait for the library streams.
+    cudaError_t je = cudaEventRecord(join_s, s_schur);
+    if (je == cudaSuccess) je = cudaStreamWaitEvent(st, join_s, 0);
+    if (je != cudaSuccess) cudaStreamSynchronize(s_schur);
+    cudaError_t jr = cudaEventRecord(join_r, s_refine);
+    if (jr == cudaSuccess) jr = cudaStreamWaitEvent(st, join_r, 0);
+    if (jr != cudaSuccess) cudaStreamSynchronize(s_refine);
+    if (e == cudaSuccess) e = je != cudaSuccess ? je : jr;
+    if (e == cudaSuccess) e = launch_dupcheck(a, st);
+    cudaEventDestroy(fork);
+    cudaEventDestroy(join_s);
+    cudaEventDestroy(join_r);
     return e;
 }
 
@@ -743,6 +821,8 @@ void load_mixed_kernels()
     load_kernel(refine_kernel<32, true>);
     load_kernel(schur32_warp_kernel<16>);
     load_kernel(refine_kernel<16, true>);
+    load_kernel(dupcheck_kernel<false>);
+    load_kernel(dupcheck_kernel<true>);
 }
 
 }  // namespace ves

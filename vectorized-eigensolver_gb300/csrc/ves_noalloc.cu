@@ -33,7 +33,10 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 // The host-side name g_noalloc_scratch is a stand-in, not a device address;
-// the address is looked up once per device, with that device current.
+// the address is looked up once per device, with that device current, and
+// kept for the life of the process (a cudaDeviceReset() of the device would
+// make it stale: the header tells callers not to use the entry point after
+// one).
 void *g_scratch_ptr[kMaxDevices] = {};
 std::mutex g_setup_mu;
 

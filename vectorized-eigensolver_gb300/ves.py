@@ -45,7 +45,11 @@ VES_SHIFTNET_LOSS_CHAMFER, VES_SHIFTNET_LOSS_ROBUST = 0, 1
 class Options(ctypes.Structure):
     _fields_ = [("precision", _int), ("max_its", _int), ("vnorm", _int), ("refine_steps", _int),
                 ("refine_tol", _dbl), ("want_vectors", _int), ("blocks_per_sm", _int), ("varsize_order", _int),
-                ("shift_sweeps", _int), ("shift_gate", ctypes.c_float), ("shift_polish", _int)]
+                ("shift_sweeps", _int), ("shift_gate", ctypes.c_float), ("shift_polish", _int),
+                ("work_counts", _VP)]
+
+
+VES_WORK_RES64, VES_WORK_CORR32, VES_WORK_RESFF, VES_WORK_POLISH, VES_WORK_COUNTS = 0, 1, 2, 3, 4
 
 
 # exported symbol -> (restype, argtypes); every name declared in include/ves.h
@@ -74,6 +78,7 @@ SIGNATURES = {
     "ves_zgemv": (_int, [_bool, _int, _int, _int, _VP, _VP, _VP, _VP, _VP, _VP, _dbl, _dbl, _VP]),
     "ves_backsubstitution": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP, _VP]),
     "ves_fp64_fma_rate": (_int, [_D, _VP]),
+    "ves_fp32_fma_rate": (_int, [_D, _VP]),
     "ves_polyroots_workspace_size": (_size, [_int, _int, _int]),
     "ves_eigensolve_varsize_workspace_size": (_size, [ctypes.c_longlong, _int, ctypes.POINTER(Options)]),
     "ves_eigensolve_varsize": (_int, [ctypes.c_longlong, _int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
@@ -156,6 +161,9 @@ def default_options(**kw):
     o = Options()
     lib().ves_default_options(ctypes.byref(o))
     for k, v in kw.items():
+        # work_counts: a device tensor of VES_WORK_COUNTS uint64/int64 counters (or a raw pointer)
+        if k == "work_counts" and hasattr(v, "data_ptr"):
+            v = v.data_ptr()
         setattr(o, k, v)
     return o
 
@@ -503,6 +511,13 @@ def fp64_fma_rate(stream=None):
     """Measured FP64 FMA throughput of the current GPU, flop/s."""
     v = ctypes.c_double(0.0)
     _check(lib().ves_fp64_fma_rate(ctypes.byref(v), _stream_ptr(stream)), "ves_fp64_fma_rate")
+    return v.value
+
+
+def fp32_fma_rate(stream=None):
+    """Measured FP32 FMA throughput of the current GPU, flop/s."""
+    v = ctypes.c_double(0.0)
+    _check(lib().ves_fp32_fma_rate(ctypes.byref(v), _stream_ptr(stream)), "ves_fp32_fma_rate")
     return v.value
 
 
