@@ -1,6 +1,12 @@
 """Benchmark: batched complex eigen-decomposition on one GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ves|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ves|reference] [--split]
+
+Several GPUs (one process per GPU under torchrun): by default every rank
+solves its own batch (seed 1 + rank; weak scaling); with --split the one batch
+is cut into contiguous ranges of whole SoA blocks (ves_partition_blocks), one
+per rank (strong scaling).  Either way the ranks share no data: a barrier and
+the max over ranks bracket the timed region.
 
 Workload (one step = one solve of the whole batch): 1,048,576 complex128
 16x16 matrices, real and imaginary parts i.i.d. N(0,1) from numpy
@@ -588,9 +594,20 @@ def run_gpu_arm(args, d):
     w = WORKLOAD
     N, n, tc = w["N"], w["n"], w["tc"]
     bc = N // tc
-    seed = rank_batch(d.rank)["seed"]  # each rank solves its own batch (weak scaling)
-    log("[bench] generating %d x %dx%d seed %d" % (N, n, n, seed))
-    rA, iA = workloads.gaussian_soa(N, n, seed, tc)
+    if args.split:
+        # strong scaling: ONE batch (seed 1) split over the ranks by whole SoA
+        # blocks (ves_partition_blocks); each rank solves its part on its own GPU
+        log("[bench] generating %d x %dx%d seed %d, split over %d ranks" % (N, n, n, w["seed"], d.world))
+        rA, iA = workloads.gaussian_soa(N, n, w["seed"], tc)
+        b0, nb = ves.partition_blocks(bc, d.world, d.rank)
+        e0, e1 = b0 * tc * n * n, (b0 + nb) * tc * n * n
+        rA, iA = rA[e0:e1].copy(), iA[e0:e1].copy()
+        N_job, N, bc = N, nb * tc, nb
+    else:
+        seed = rank_batch(d.rank)["seed"]  # each rank solves its own batch (weak scaling)
+        log("[bench] generating %d x %dx%d seed %d" % (N, n, n, seed))
+        rA, iA = workloads.gaussian_soa(N, n, seed, tc)
+        N_job = N * d.world
     dAr = torch.from_numpy(rA).cuda()
     dAi = torch.from_numpy(iA).cuda()
     dEr = torch.empty(N * n, dtype=torch.float64, device="cuda")
@@ -632,7 +649,7 @@ def run_gpu_arm(args, d):
     ms = e0.elapsed_time(e1)
     ck = clocks.stop()
     ms_max = d.max(ms)
-    value = N * d.world * args.steps / (ms_max * 1e-3)
+    value = N_job * args.steps / (ms_max * 1e-3)
 
     # statistics + verification (outside the timed region)
     step(with_stats=True)
@@ -701,11 +718,13 @@ def run_gpu_arm(args, d):
         return
     out = {
         "metric": METRIC, "value": value, "unit": "eigensolves/s", "n_gpus": d.world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic: complex Gaussian N(0,1)+iN(0,1), numpy default_rng(seed 1 + rank)",
-        "config": {"workload": "1,048,576 complex128 16x16 per GPU, SoA thread_cnt=512, plain FP64 "
-                               "(zgehrd->zunghr->zlahqr->ztrevc)", "n": n, "n_matrices": N, "thread_cnt": tc,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "strong" if args.split else "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: complex Gaussian N(0,1)+iN(0,1), numpy default_rng(%s)"
+                % ("1, split over the ranks by SoA blocks" if args.split else "seed 1 + rank"),
+        "config": {"workload": "1,048,576 complex128 16x16 %s, SoA thread_cnt=512, plain FP64 "
+                               "(zgehrd->zunghr->zlahqr->ztrevc)" % ("in total" if args.split else "per GPU"),
+                   "n": n, "n_matrices": N_job, "thread_cnt": tc,
                    "form": "plain FP64", "l2": "inputs (4.3 GB) larger than L2; no flush",
                    "sweeps_per_eigenvalue": s_mean},
         "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak_fp64 / 1e12, "unit": "TFLOP/s",
@@ -847,6 +866,9 @@ def main():
     ap.add_argument("--impl", default="ves", choices=["ves", "reference"])
     ap.add_argument("--ref-sample", type=int, default=65_536,
                     help="matrices per step of the CPU reference arm (a prefix of the batch)")
+    ap.add_argument("--split", action="store_true",
+                    help="strong scaling: split the one 1,048,576-matrix batch over the ranks (default: weak, "
+                         "every rank solves its own batch)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true",

@@ -238,9 +238,10 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt,
 
 /* The shift network: features [family parameters (n_params per matrix, a
  * row-major FP64 device array), optional sin/cos features of them, Re diag A,
- * Im diag A] -> n predicted eigenvalues; hidden layers of `hidden` units, GELU,
- * BF16 on the tcgen05 tensor cores; an FP32 output layer.  Trained on eigenvalues from the FP64
- * solver (rE, iE in the SoA layout of rA, iA) with a permutation-invariant
+ * Im diag A, optional subdiagonal norms] -> n predicted eigenvalues; hidden
+ * layers of `hidden` units, GELU, BF16 on the tcgen05 tensor cores; an FP32
+ * output layer.  Trained on eigenvalues from the FP64 solver (rE, iE in the
+ * SoA layout of rA, iA) with a permutation-invariant
  * loss (symmetric Chamfer distance between the predicted and the true
  * eigenvalue sets), Adam with cosine learning-rate decay from lr to lr/50 over
  * the call's epochs.  Checkpoints are flat binary. */
@@ -257,6 +258,7 @@ typedef struct ves_shiftnet_config {
                     * (sqrt(d^2 + delta^2) - delta per matched pair) */
     float delta;   /* robust loss scale in standardised units; default 0.01 */
     unsigned long long seed;  /* weight initialisation */
+    int subdiag;   /* 1: also the 2-norms of the n - 1 subdiagonals of A as features; default 0 */
 } ves_shiftnet_config;
 void ves_shiftnet_default_config(ves_shiftnet_config *cfg);
 int ves_shiftnet_create_config(ves_shiftnet **net, const ves_shiftnet_config *cfg);
@@ -266,6 +268,18 @@ void ves_shiftnet_destroy(ves_shiftnet *net);
 int ves_shiftnet_train(ves_shiftnet *net, long long count, int thread_cnt, const double *params,
                        const double *rA, const double *iA, const double *rE, const double *iE,
                        int epochs, int batch, float lr, unsigned long long seed, float *loss_per_epoch, void *stream);
+/* Number of parameters (floats): W and b of every layer, W row-major out x in. */
+size_t ves_shiftnet_param_count(const ves_shiftnet *net);
+/* The loss and its gradient over ONE batch of all `count` matrices (32 <= count
+ * <= 65536, a multiple of thread_cnt) at the network's current weights and
+ * standardisation, computed as a training step computes them (hidden layers:
+ * tcgen05 BF16 GEMMs with FP32 accumulation; output layer: FP32).  grad
+ * (device, ves_shiftnet_param_count floats) receives the gradients in
+ * checkpoint order (W then b of layer 0, 1, ...); loss (device, one float) the
+ * batch loss.  Synchronous.  For tests and tooling. */
+int ves_shiftnet_gradient(const ves_shiftnet *net, long long count, int thread_cnt, const double *params,
+                          const double *rA, const double *iA, const double *rE, const double *iE, float *grad,
+                          float *loss, void *stream);
 size_t ves_shiftnet_predict_workspace_size(const ves_shiftnet *net, long long count);
 int ves_shiftnet_predict(const ves_shiftnet *net, long long count, int thread_cnt, const double *params,
                          const double *rA, const double *iA, double *rS, double *iS,
@@ -357,6 +371,18 @@ int ves_fp32_fma_rate(double *flops_per_s, void *stream);
 int ves_eigensolve_noalloc(int dim, int block_cnt, int thread_cnt,
                            const double *rA, const double *iA, double *rE, double *iE, double *rV, double *iV,
                            int *status, void *stream);
+
+/* One batch over several GPUs (no counterpart in the reference, which runs on
+ * one device): the batch is split into `parts` contiguous ranges of whole SoA
+ * blocks, sizes differing by at most one block; part `part` (0-based) owns
+ * blocks [*first_block, *first_block + *n_blocks).  Whole blocks are
+ * contiguous in every plane, so a part is the caller's arrays offset by
+ * first_block * thread_cnt * dim * dim (matrices) or first_block * thread_cnt
+ * * dim (vectors), solved by any entry point above with block_cnt = n_blocks
+ * on that part's own GPU (one process or host thread per GPU; the parts share
+ * nothing, so no collective is involved).  Host arithmetic only.  Returns
+ * VES_ERR_ARG for block_cnt < 0, parts < 1 or part outside [0, parts). */
+int ves_partition_blocks(int block_cnt, int parts, int part, int *first_block, int *n_blocks);
 
 /* Last error message of the calling thread ("" if none). */
 const char *ves_last_error(void);

@@ -134,3 +134,29 @@ def test_device_transposes(n, N, tc):
     ves.complex_from_soa_vec_dev(n, bc, tc, r2, i2, out)
     torch.cuda.synchronize()
     assert torch.equal(out, dv)
+
+
+def test_split_batch_equals_one_call():
+    """One batch solved as 3 parts of whole SoA blocks (ves_partition_blocks, the
+    split each GPU of a multi-GPU job takes) gives the one-call result bit for
+    bit: every matrix is solved by the same lane code whatever the launch."""
+    import torch
+    n, tc, bc = 12, 64, 50
+    N = bc * tc
+    rng = np.random.default_rng(77)
+    A = rng.standard_normal((N, n, n)) + 1j * rng.standard_normal((N, n, n))
+    rA, iA = ves.soa_from_complex(A, tc)
+    dA = [torch.from_numpy(x).cuda() for x in (rA, iA)]
+    whole = [torch.empty(N * n, dtype=torch.float64, device="cuda") for _ in range(2)] + \
+            [torch.empty_like(dA[0]) for _ in range(2)]
+    ves.eigensolve(n, bc, tc, dA[0], dA[1], *whole)
+    parts = [torch.empty_like(t) for t in whole]
+    for p in range(3):
+        first, nb = ves.partition_blocks(bc, 3, p)
+        m0, m1 = first * tc * n * n, (first + nb) * tc * n * n
+        v0, v1 = first * tc * n, (first + nb) * tc * n
+        ves.eigensolve(n, nb, tc, dA[0][m0:m1], dA[1][m0:m1], parts[0][v0:v1], parts[1][v0:v1],
+                       parts[2][m0:m1], parts[3][m0:m1])
+    torch.cuda.synchronize()
+    for a, b in zip(whole, parts):
+        assert torch.equal(a, b)

@@ -56,10 +56,15 @@ def test_exact_and_garbage_predictions(n):
     assert fb.sum().item() > 0 and ((st & ves.VES_STATUS_SHIFT_FALLBACK) != 0).any()
 
 
-def test_train_predict_checkpoint():
+@pytest.mark.parametrize("subdiag", [0, 1])
+def test_train_predict_checkpoint(subdiag):
+    """Training lowers the loss and beats the trivial diag(A) guess; a saved
+    checkpoint (with or without the subdiagonal-norm features) predicts the
+    same bits after loading."""
     import torch
     n, N = 8, 16384
-    net, losses = learned_shift.train(n, count=N, epochs=8, batch=512, lr=2e-3, hidden=128, param_seed=21)
+    net, losses = learned_shift.train(n, count=N, epochs=8, batch=512, lr=2e-3, hidden=128, param_seed=21,
+                                      subdiag=subdiag)
     assert np.isfinite(losses).all()
     assert losses[-1] < 0.5 * losses[0]
     p, rA, iA = learned_shift.family(4096, n, param_seed=22)

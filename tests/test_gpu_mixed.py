@@ -175,15 +175,20 @@ def test_mixed_fullsize_n32():
         assert (err / nA).max() <= 1e-12
 
 
-@pytest.mark.parametrize("n", [2, 3, 9, 12, 16, 24, 31, 32])
-@pytest.mark.parametrize("mode", ["lane", "warp", "warp32"])
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 9, 12, 16, 24, 31, 32])
+@pytest.mark.parametrize("mode", ["lane", "warp", "warp32", "group4", "group8"])
 def test_mixed_schur_kernels(n, mode, monkeypatch):
-    """Every FP32 Schur kernel (lane per matrix; a matrix per half warp for
-    n <= 16 or per warp, in shared memory) meets the bar, with thread_cnt not
-    a multiple of the warp and a batch (203) that is not a multiple of a
-    block's matrices, so the last warp's two halves get one matrix."""
+    """Every FP32 Schur kernel (lane per matrix; a matrix per group of 4 or 8
+    lanes, per half warp or per warp, in shared memory) meets the bar, with
+    thread_cnt not a multiple of the warp and a batch (203) that is not a
+    multiple of a block's matrices, so the last warp's groups are partly
+    empty."""
     if mode == "warp32" and n > 16:
         pytest.skip("the same kernel as mode warp for n > 16")
+    if mode.startswith("group") and n > 16:
+        pytest.skip("the group kernels take n <= 16")
+    if n == 1 and mode != "lane" and not mode.startswith("group"):
+        pytest.skip("covered by the lane and group kernels")
     monkeypatch.setenv("VES_MIXED_SCHUR", mode)
     rng = np.random.default_rng(4000 + n)
     N, tc = 203, 7
@@ -259,9 +264,9 @@ def test_mixed_close_clusters_no_duplicate_eigenvalues():
 
 
 def test_mixed_work_counters():
-    """work_counts: one float-float residual per refined pair, at least one
-    FP64 residual and one FP32 correction per pair; nothing counted without
-    the option."""
+    """work_counts: two float-float residuals per refined pair (the ones that
+    drive the first two corrections), at least one FP64 residual (the one that
+    accepts) and two corrections per pair; no polish steps in this form."""
     import torch
     rng = np.random.default_rng(31)
     n, N, tc = 12, 512, 32
@@ -271,8 +276,8 @@ def test_mixed_work_counters():
     fb = int(((out["status"] & ves.VES_STATUS_REFINE_FALLBACK) != 0).sum())
     res64, corr, ff, polish = (int(x) for x in wc.cpu())
     pairs = (N - fb) * n
-    assert ff == pairs
-    assert pairs <= res64 <= 9 * pairs and pairs <= corr <= 9 * pairs
+    assert ff == 2 * pairs
+    assert pairs <= res64 <= 7 * pairs and 3 * pairs <= corr <= 9 * pairs
     assert polish == 0
 
 

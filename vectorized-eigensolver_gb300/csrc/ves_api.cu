@@ -237,6 +237,7 @@ cudaStream_t pipeline_stream(int k)
 // every matrix is solved by the same lane code whatever the grid.
 bool do_eigensolver(int dim, int bc, int tc, double *rA, double *iA, double *rE, double *iE, double *rV, double *iV)
 {
+    ves::NvtxRange range("ves eigensolver (drop-in)");
     ves::Geom g;
     if (!geom_ok(dim, bc, tc, &g)) return false;
     if (g.N == 0) return true;
@@ -266,6 +267,7 @@ bool do_eigensolver(int dim, int bc, int tc, double *rA, double *iA, double *rE,
         nb = std::min<long long>(cb, bc - b0);
     };
     auto copy_in_and_solve = [&](long long c) -> bool {
+        ves::NvtxRange r("ves chunk: copy in + solve");
         long long b0, nb;
         chunk(c, b0, nb);
         cudaStream_t s = st[c & 1];
@@ -285,6 +287,7 @@ bool do_eigensolver(int dim, int bc, int tc, double *rA, double *iA, double *rE,
         return cuda_ok(ves::launch_fused_fp64(a, s), "eigensolver kernel launch");
     };
     auto copy_out = [&](long long c) -> bool {
+        ves::NvtxRange r("ves chunk: copy out");
         long long b0, nb;
         chunk(c, b0, nb);
         cudaStream_t s = st[c & 1];
@@ -301,6 +304,7 @@ bool do_eigensolver(int dim, int bc, int tc, double *rA, double *iA, double *rE,
         if (c + 1 < nchunks) ok = copy_in_and_solve(c + 1);
         ok = ok && copy_out(c);
     }
+    ves::NvtxRange wait("ves eigensolver: wait");
     const bool s0 = cuda_ok(cudaStreamSynchronize(st[0]), "eigensolver stream 0");
     const bool s1 = cuda_ok(cudaStreamSynchronize(st[1]), "eigensolver stream 1");
     return ok && s0 && s1;
@@ -633,6 +637,7 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
                    void *workspace, size_t workspace_bytes, void *stream)
 {
     begin_call();
+    ves::NvtxRange range("ves_eigensolve");
     ves::Geom g;
     if (!geom_ok(dim, block_cnt, thread_cnt, &g)) return VES_ERR_ARG;
     if (g.N == 0) return VES_OK;
@@ -720,6 +725,10 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
     m.fb_count = count;
     m.blocks_per_sm = o.blocks_per_sm;
     m.work = o.work_counts;
+    // refinement steps with a float-float residual: 2 (default) or 1; VES_MIXED_FF_STEPS overrides (tuning)
+    m.ff_steps = 2;
+    if (const char *ff = getenv("VES_MIXED_FF_STEPS"))
+        if (ff[0] == '1' || ff[0] == '2') m.ff_steps = ff[0] - '0';
     // The Schur stage of one chunk overlaps the refinement of the previous one on
     // two library streams (forked from and joined back into the caller's);
     // VES_MIXED_OVERLAP=0 runs the two stages one after the other on the caller's
@@ -1118,6 +1127,19 @@ int ves_fp32_fma_rate(double *flops_per_s, void *stream)
     begin_call();
     if (!flops_per_s) { set_error("null pointer"); return VES_ERR_ARG; }
     return native(cuda_ok(ves::fp32_fma_rate(flops_per_s, (cudaStream_t)stream), "fp32 probe"));
+}
+
+int ves_partition_blocks(int block_cnt, int parts, int part, int *first_block, int *n_blocks)
+{
+    if (block_cnt < 0 || parts < 1 || part < 0 || part >= parts || !first_block || !n_blocks) {
+        set_error("ves_partition_blocks: need block_cnt >= 0, parts >= 1, 0 <= part < parts");
+        return VES_ERR_ARG;
+    }
+    // the first (block_cnt % parts) parts get one block more
+    const int base = block_cnt / parts, extra = block_cnt % parts;
+    *n_blocks = base + (part < extra ? 1 : 0);
+    *first_block = part * base + (part < extra ? part : extra);
+    return VES_OK;
 }
 
 const char *ves_last_error(void) { return t_last_error.c_str(); }

@@ -3,10 +3,21 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <cstddef>
 #include <cstdlib>
 
 namespace ves {
+
+// An NVTX range for the lifetime of the object: the host-side stages of the
+// entry points (copies, launches) show up named in Nsight Systems.  NVTX is
+// header-only and costs a pointer test when no tool is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Batch geometry of the reference's SoA layout: N = block_cnt * thread_cnt
 // matrices of order n, interleave stride tc = thread_cnt.
@@ -64,6 +75,7 @@ struct MixedArgs {
     // ends inside the batch); launch_mixed sets the whole batch when m_end == 0
     long long m_begin, m_end;
     unsigned long long *work;  // optional work counters (WORK_*)
+    int ff_steps;              // refinement steps whose residual is float-float (1 or 2)
 };
 
 size_t mixed_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blocks, int *out_threads);

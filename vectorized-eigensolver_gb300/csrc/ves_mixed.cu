@@ -102,6 +102,48 @@ __device__ __forceinline__ void ff_mac(float &s, float &e, const float a, const 
     e = __fadd_rn(e, pe);
 }
 
+// r = A v - lambda v in float-float on the FP32 pipe, into r32 (rounded to
+// FP32).  A = Ah + Al (two FP32 parts), v = vh + vl and lambda = lh + ll
+// (FP32 heads and tails; kLo = false: the tails are zero).  The head products
+// Ah vh and lh vh split exactly into rounded products and their errors (fma),
+// the rounded products are summed by TwoSum, and the errors, Ah vl, Al vh,
+// lh vl and ll vh are summed in FP32 beside them; Al vl and ll vl (~2^-48 of
+// the terms) are dropped.  Error ~ 2^-48 ||A|| ||v||.
+template <int MAXN, bool kLo, class MB>
+__device__ __forceinline__ void ff_residual(const int n, const MB &Ah, const MB &Al, const cx<float> *vh,
+                                            const cx<float> *vl, const cx<float> lh, const cx<float> ll,
+                                            cx<float> *r32)
+{
+    for (int i = 1; i <= n; ++i) {
+        const cx<float> vi = vh[i - 1];
+        float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f;
+        ff_mac(sr, er, -lh.r, vi.r);
+        ff_mac(sr, er, lh.i, vi.i);
+        ff_mac(si, ei, -lh.r, vi.i);
+        ff_mac(si, ei, -lh.i, vi.r);
+        if (kLo) {
+            const cx<float> wi = vl[i - 1];
+            er = fmaf(lh.i, wi.i, fmaf(-lh.r, wi.r, fmaf(ll.i, vi.i, fmaf(-ll.r, vi.r, er))));
+            ei = fmaf(-lh.i, wi.r, fmaf(-lh.r, wi.i, fmaf(-ll.i, vi.r, fmaf(-ll.r, vi.i, ei))));
+        }
+        for (int j = 1; j <= n; ++j) {
+            const cx<float> ah = Ah.ld(i, j), al = Al.ld(i, j), vj = vh[j - 1];
+            ff_mac(sr, er, ah.r, vj.r);
+            ff_mac(sr, er, -ah.i, vj.i);
+            ff_mac(si, ei, ah.r, vj.i);
+            ff_mac(si, ei, ah.i, vj.r);
+            er = fmaf(-al.i, vj.i, fmaf(al.r, vj.r, er));
+            ei = fmaf(al.i, vj.r, fmaf(al.r, vj.i, ei));
+            if (kLo) {
+                const cx<float> wj = vl[j - 1];
+                er = fmaf(-ah.i, wj.i, fmaf(ah.r, wj.r, er));
+                ei = fmaf(ah.i, wj.r, fmaf(ah.r, wj.i, ei));
+            }
+        }
+        r32[i - 1] = mk(__fadd_rn(sr, er), __fadd_rn(si, ei));
+    }
+}
+
 __device__ __forceinline__ void to_fp64_list(const MixedArgs &a, int *flags, long long m)
 {
     // the first pair (or the Schur kernel) to give up on matrix m puts it on the list
@@ -363,6 +405,299 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
     }
 }
 
+// ---------------------------------------------------------------------------
+// schur32_group_kernel<G>: the FP32 Schur stage for n <= 16 with one matrix
+// per group of G lanes (G = 4: eight matrices per warp; G = 8: four), H and Z
+// in shared memory (4.5 KB per matrix at n = 16).
+//
+// Why: the lane kernel above keeps T and Z of its 32 matrices per warp in an
+// HBM buffer, and its QR sweeps stream that buffer through DRAM (about 245 KB
+// of traffic per matrix at n = 16 against 8.4 KB of input and output): it is
+// memory-latency bound with the FP32 pipe below 10% busy.  A matrix per warp
+// or half warp keeps H and Z on chip but runs every scalar step of a
+// reflector on 16-32 lanes for one matrix, and its lanes idle on the short
+// rows near the end of a sweep.  Here a group of G lanes owns a matrix: lane
+// q of a group handles rows and columns q + 1, q + 1 + G, ... of every
+// element-wise update, the scalar steps (reflector, shift, deflation test)
+// run redundantly on the G lanes, and the warp's 32 / G matrices move in
+// lockstep per QR sweep, as the lane kernel's 32 do: every group keeps its
+// own active block [L, I] and sweep count, the bulge-chase step K is
+// warp-uniform over the union of the groups' windows, and a group whose
+// window does not contain K idles for that step.  Values that all lanes of a
+// group write to one location (a zeroed subdiagonal, a reflector's leading
+// entry) are computed identically on every lane, so no lane can read a stale
+// copy.
+//
+// Same algorithm per element as the lane routines (zgehd2, zung2r, zlahqr
+// single shift with the FP64 deflation test, ztrevc back substitution), in a
+// different summation order for the reflector norms; the output is the
+// per-matrix buffer layout of schur32_warp_kernel, read by refine_kernel.
+// ---------------------------------------------------------------------------
+constexpr int kGroupSchurThreads = 64;  // 2 warps per block
+
+// float2 per matrix slot: H and Z (n (n + 1) each), tau (n), padded so that
+// the slots of one warp start 4 (G = 4) or 8 (G = 8) float2 apart modulo 16:
+// the lanes of a warp then touch distinct shared-memory banks when every
+// group accesses the same element of its own matrix
+__host__ __device__ __forceinline__ int group_slot(int n, int G)
+{
+    const int raw = 2 * n * (n + 1) + n, want = G == 4 ? 4 : 8;
+    return raw + ((want - raw % 16) + 16) % 16;
+}
+__host__ __device__ __forceinline__ size_t group_schur_smem(int n, int G)
+{
+    return (size_t)(kGroupSchurThreads / G) * group_slot(n, G) * sizeof(float2);
+}
+
+template <int G>
+__global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const MixedArgs a, float2 *buf, int *flags)
+{
+    extern __shared__ float2 gsm[];
+    constexpr int MPW = 32 / G;  // matrices per warp
+    const int n = a.g.n, tc = a.g.tc;
+    const int lane = threadIdx.x & 31, gl = lane & (G - 1), j0 = gl + 1;
+    const unsigned gmask = group_mask<G>(lane);
+    const int lda = n + 1;
+    float2 *sH = gsm + (size_t)(threadIdx.x / G) * group_slot(n, G);
+    float2 *sZ = sH + n * lda, *sTau = sZ + n * lda;
+    const SmemMat H{sH, lda}, Z{sZ, lda};
+    const long long nn = (long long)n * n;
+    const float ulp = lim<float>::eps();
+    const float smlnum = lim<float>::tiny() * ((float)n / ulp);
+    const long long wg = (long long)blockIdx.x * (kGroupSchurThreads / 32) + (threadIdx.x >> 5);
+    const long long nw = (long long)gridDim.x * (kGroupSchurThreads / 32);
+
+    for (long long base = a.m_begin + wg * MPW; base < a.m_end; base += nw * MPW) {
+        const long long m = base + (lane / G);
+        const bool valid = m < a.m_end;
+        // ---- load A (FP64 SoA) into H as FP32; Ah, Al to the buffer
+        const long long mo = valid ? soa_off_m(m, nn, tc) : 0;
+        float2 *out = buf + (valid ? m : 0) * mat_elems(n);
+        bool bad = false;
+        float s2 = 0.f;
+        for (int e = gl; e < nn; e += G) {
+            float2 h = make_float2(0.f, 0.f);
+            if (valid) {
+                const long long k = mo + (long long)e * tc;
+                const double re = a.rA[k], im = a.iA[k];
+                bad |= nonfinite(re) | nonfinite(im);
+                h = make_float2((float)re, (float)im);
+                s2 = fmaf(h.y, h.y, fmaf(h.x, h.x, s2));
+                out[3 * nn + n + e] = h;
+                out[4 * nn + n + e] = make_float2((float)(re - (double)h.x), (float)(im - (double)h.y));
+            }
+            sH[(e % n) + (e / n) * lda] = h;
+        }
+        const float nA2 = group_sum<G>(s2, gmask);
+        const bool fb = valid && (__any_sync(gmask, bad) || !(nA2 < 1e36f));
+        const bool run = valid && !fb;
+        if (!run)  // a zero matrix: harmless arithmetic, and no sweeps
+            for (int e = gl; e < nn; e += G) sH[(e % n) + (e / n) * lda] = make_float2(0.f, 0.f);
+        __syncwarp();
+
+        // ---- zgehd2: reflector i from column i, applied right then left
+        for (int i = 1; i <= n - 1; ++i) {
+            const int mm = n - i;
+            float xs = 0.f;
+            for (int k = j0; k <= n; k += G)
+                if (k >= i + 2) { const cx<float> x = H.ld(k, i); xs = fmaf(x.i, x.i, fmaf(x.r, x.r, xs)); }
+            const float xnorm2 = group_sum<G>(xs, gmask);
+            const cx<float> alpha = H.ld(i + 1, i);
+            const bool trivial = (xnorm2 == 0.f) && (alpha.i == 0.f);
+            const float beta = trivial ? alpha.r : -copysignf(sqrtf(fmaf(alpha.r, alpha.r, fmaf(alpha.i, alpha.i, xnorm2))), alpha.r);
+            cx<float> t = mk(0.f, 0.f), scale = mk(0.f, 0.f);
+            if (!trivial) {
+                const float rb = 1.f / beta;
+                t = mk((beta - alpha.r) * rb, -alpha.i * rb);
+                scale = cinv(mk(alpha.r - beta, alpha.i));
+            }
+            __syncwarp(gmask);  // every lane has read column i
+            for (int k = j0; k <= n; k += G)
+                if (k >= i + 2) H.st(k, i, cmul(H.ld(k, i), scale));
+            sTau[i - 1] = make_float2(t.r, t.i);
+            __syncwarp(gmask);
+            for (int r = j0; r <= n; r += G) {  // right: row r of A(1:n, i+1:n) -= tau (A v)_r v^H
+                cx<float> sacc = H.ld(r, i + 1);
+                for (int q = 2; q <= mm; ++q) sacc = cmac(sacc, H.ld(r, i + q), H.ld(i + q, i));
+                const cx<float> ts = cmul(t, sacc);
+                H.st(r, i + 1, csub(H.ld(r, i + 1), ts));
+                for (int q = 2; q <= mm; ++q) H.st(r, i + q, cnmacc(H.ld(r, i + q), ts, H.ld(i + q, i)));
+            }
+            __syncwarp(gmask);
+            const cx<float> tcj = conj(t);
+            for (int c = j0; c <= n; c += G) {  // left: column c of A(i+1:n, i+1:n) -= conj(tau) v (v^H A)_c
+                if (c < i + 1) continue;
+                cx<float> sacc = H.ld(i + 1, c);
+                for (int q = 2; q <= mm; ++q) sacc = cjmac(sacc, H.ld(i + q, i), H.ld(i + q, c));
+                const cx<float> ts = cmul(tcj, sacc);
+                H.st(i + 1, c, csub(H.ld(i + 1, c), ts));
+                for (int q = 2; q <= mm; ++q) H.st(i + q, c, cnmac(H.ld(i + q, c), H.ld(i + q, i), ts));
+            }
+            __syncwarp(gmask);
+            H.st(i + 1, i, mk(beta, 0.f));
+            __syncwarp(gmask);
+        }
+        // ---- zung2r: Z = Q from the reflectors, last reflector first
+        for (int e = gl; e < nn; e += G) sZ[(e % n) + (e / n) * lda] = make_float2(0.f, 0.f);
+        __syncwarp(gmask);
+        for (int i = n - 1; i >= 1; --i) {
+            const cx<float> t = mk(sTau[i - 1].x, sTau[i - 1].y);
+            const int c = i + 1;
+            for (int j = j0; j <= n; j += G) {
+                if (j < c + 1) continue;
+                cx<float> sacc = Z.ld(c, j);
+                for (int k = c + 1; k <= n; ++k) sacc = cjmac(sacc, H.ld(k, i), Z.ld(k, j));
+                const cx<float> ts = cmul(t, sacc);
+                Z.st(c, j, csub(Z.ld(c, j), ts));
+                for (int k = c + 1; k <= n; ++k) Z.st(k, j, cnmac(Z.ld(k, j), H.ld(k, i), ts));
+            }
+            __syncwarp(gmask);
+            for (int j = j0; j <= n; j += G) {
+                if (j >= c + 1) Z.st(j, c, cmul(H.ld(j, i), mk(-t.r, -t.i)));
+                if (j == c) Z.st(c, c, mk(1.f - t.r, -t.i));
+                if (j >= 2 && j <= c - 1) Z.st(j, c, mk(0.f, 0.f));
+            }
+            __syncwarp(gmask);
+        }
+        for (int j = j0; j <= n; j += G) {
+            Z.st(j, 1, mk(j == 1 ? 1.f : 0.f, 0.f));
+            if (j > 1) Z.st(1, j, mk(0.f, 0.f));
+            for (int k = j + 2; k <= n; ++k) H.st(k, j, mk(0.f, 0.f));  // clear below the subdiagonal
+        }
+        __syncwarp(gmask);
+        // ---- make the subdiagonal real
+        for (int i = 2; i <= n; ++i) {
+            const cx<float> h = H.ld(i, i - 1);
+            __syncwarp(gmask);
+            if (h.i != 0.f) {  // the same on every lane of the group
+                cx<float> sc = cscal(h, 1.f / cabs1(h));
+                sc = cscal(conj(sc), 1.f / cabs(sc));
+                H.st(i, i - 1, mk(cabs(h), 0.f));
+                for (int j = j0; j <= n; j += G)
+                    if (j >= i) H.st(i, j, cmul(H.ld(i, j), sc));
+                __syncwarp(gmask);
+                const int re = (i + 1) < n ? (i + 1) : n;
+                for (int j = j0; j <= n; j += G) {  // column i, H(i, i) included (|sc| = 1)
+                    if (j <= re) H.st(j, i, cmulc(H.ld(j, i), sc));
+                    Z.st(j, i, cmulc(Z.ld(j, i), sc));
+                }
+            }
+            __syncwarp(gmask);
+        }
+        __syncwarp();
+
+        // ---- single-shift QR, the warp's groups in lockstep per sweep
+        int I = n, L = 1, its = 0, status = 0, sweeps = 0;
+        bool done = !run || n <= 1;
+        for (;;) {
+            bool sweep = false;
+            cx<float> v0 = mk(0.f, 0.f), v1 = mk(0.f, 0.f);
+            if (!done) {
+                for (;;) {
+                    if (I <= 1) { done = true; break; }
+                    if (its > a.max_its) { status |= ST_ITCAP; --I; L = 1; its = 0; continue; }
+                    L = deflation_scan64(I, L, H, n, ulp, smlnum);
+                    if (L > 1) H.st(L, L - 1, mk(0.f, 0.f));  // every lane of the group: the same value
+                    if (L >= I) { --I; L = 1; its = 0; continue; }
+                    const cx<float> t = qr_shift<float>(I, L, its, H);
+                    const cx<float> h11s = csub(H.ld(L, L), t);
+                    const float h21 = H.ld(L + 1, L).r;
+                    const float rs = 1.f / (cabs1(h11s) + fabsf(h21));
+                    v0 = cscal(h11s, rs);
+                    v1 = mk(h21 * rs, 0.f);
+                    sweep = true;
+                    ++its;
+                    ++sweeps;
+                    break;
+                }
+            }
+            if (!__any_sync(FULL, sweep)) break;
+            const int Kmin = __reduce_min_sync(FULL, sweep ? L : INT_MAX);
+            const int Kmax = __reduce_max_sync(FULL, sweep ? I - 1 : 0);
+            __syncwarp();  // the scans and shifts have read H
+            for (int K = Kmin; K <= Kmax; ++K) {
+                const bool act = sweep && K >= L && K <= I - 1;
+                cx<float> a0 = v0, a1 = v1, t1 = mk(0.f, 0.f);
+                if (act) {
+                    if (K > L) { a0 = H.ld(K, K - 1); a1 = H.ld(K + 1, K - 1); }
+                    zlarfg2<float>(a0, a1, t1);
+                }
+                __syncwarp();  // every lane has read H(K, K-1), H(K+1, K-1)
+                if (act && K > L) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(0.f, 0.f)); }
+                const cx<float> w1 = a1, cw = conj(w1), c1 = conj(t1);
+                const float t2 = fmaf(t1.r, w1.r, -(t1.i * w1.i));
+                if (act) {
+                    for (int j = K + gl; j <= n; j += G) {  // rows K, K+1, columns K..n
+                        cx<float> h1 = H.ld(K, j), h2 = H.ld(K + 1, j);
+                        rot_pair(h1, h2, c1, t2, w1);
+                        H.st(K, j, h1);
+                        H.st(K + 1, j, h2);
+                    }
+                    for (int j = j0; j <= n; j += G) {  // Schur vectors: columns K, K+1
+                        cx<float> z1 = Z.ld(j, K), z2 = Z.ld(j, K + 1);
+                        rot_pair(z1, z2, t1, t2, cw);
+                        Z.st(j, K, z1);
+                        Z.st(j, K + 1, z2);
+                    }
+                }
+                __syncwarp();  // the row update is done: the column update shares the 2 x 2 block
+                if (act) {
+                    const int je = (K + 2) < I ? (K + 2) : I;
+                    for (int j = j0; j <= je; j += G) {  // columns K, K+1, rows 1..min(K+2, I)
+                        cx<float> h1 = H.ld(j, K), h2 = H.ld(j, K + 1);
+                        rot_pair(h1, h2, t1, t2, cw);
+                        H.st(j, K, h1);
+                        H.st(j, K + 1, h2);
+                    }
+                }
+                __syncwarp();
+            }
+            // make H(I, I-1) real (the groups that swept)
+            const cx<float> h = sweep ? H.ld(I, I - 1) : mk(0.f, 0.f);
+            __syncwarp();
+            if (sweep && h.i != 0.f) {
+                const float d = cabs(h);
+                const cx<float> z = conj(cscal(h, 1.f / d));
+                H.st(I, I - 1, mk(d, 0.f));
+                for (int j = j0; j <= n; j += G) {
+                    if (j >= I + 1) H.st(I, j, cmul(H.ld(I, j), z));
+                    if (j <= I - 1) H.st(j, I, cmulc(H.ld(j, I), z));
+                    Z.st(j, I, cmulc(Z.ld(j, I), z));
+                }
+            }
+            __syncwarp();
+        }
+        const bool to64 = fb || (status & ST_ITCAP);
+        // ---- T (upper triangle) and Z to the buffer, then the T-eigenvectors into sZ
+        if (valid && !to64)
+            for (int e = gl; e < nn; e += G) {
+                const int r = e % n, c = e / n;
+                out[e] = r <= c ? sH[r + c * lda] : make_float2(0.f, 0.f);
+                out[nn + e] = sZ[r + c * lda];
+            }
+        __syncwarp();
+        for (int j = j0; j <= n; j += G) {  // lane solves columns j0, j0 + G, ... (T read only)
+            const SmemCol xc{sZ + (j - 1) * lda};
+            const cx<float> tkk = H.ld(j, j);
+            const float smin = fmaxf(ulp * cabs1(tkk), smlnum);
+            const float sc = j > 1 ? trevc_solve<float>(j, H, xc, smin, tkk) : 1.f;
+            xc.st(j, mk(sc, 0.f));
+            for (int i = j + 1; i <= n; ++i) xc.st(i, mk(0.f, 0.f));
+        }
+        __syncwarp();
+        if (valid && !to64)
+            for (int e = gl; e < nn; e += G) out[2 * nn + e] = sZ[(e % n) + (e / n) * lda];
+        if (valid && gl == 0) {
+            out[3 * nn] = make_float2(nA2, 0.f);  // ||A||_F^2 for the refinement's tolerance
+            flags[m] = to64 ? 1 : 0;
+            if (to64) to_fp64_list(a, flags, m);
+            if (a.status) a.status[m] = status;
+            if (a.sweeps) a.sweeps[m] = sweeps;
+        }
+        __syncwarp();
+    }
+}
+
 // FP32 matrix in the Schur buffer, element stride S: 32 in the group layout
 // of schur32_kernel, 1 in the per-matrix layout of schur32_warp_kernel.
 template <int S> struct MatBuf {
@@ -401,7 +736,7 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
     const MatSoA<double> A{const_cast<double *>(a.rA) + mo, const_cast<double *>(a.iA) + mo, tc, n};
 
     cx<double> v[MAXN];
-    cx<float> r32[MAXN], dx[MAXN];
+    cx<float> r32[MAXN], dx[MAXN], vl[MAXN];
     cx<double> lam = mk(0.0, 0.0);
     if (act) {
         lam = up(T.ld(k, k));
@@ -419,37 +754,31 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
     const float xkk = act ? X.ld(k, k).r : 1.f;
     bool fail = false;
     int n_res64 = 0, n_corr = 0, n_ff = 0;  // work counters: FP64 / float-float residuals, FP32 corrections
+    const int ff_steps = a.max_steps >= 2 ? a.ff_steps : 1;  // steps whose residual is float-float
     for (int step = 0; step <= a.max_steps; ++step) {
         if (!__any_sync(FULL, act)) break;
         if (!act) continue;
         bool certified = false;
-        n_res64 += step > 0;
-        n_ff += step == 0;
-        if (step == 0) {
-            // First residual in float-float on the FP32 pipe: v0 and lambda0 are
-            // FP32 numbers and A = Ah + Al, so every product splits exactly into
-            // a rounded product and its error; the rounded products are summed
-            // by TwoSum, the rest in FP32.  Error ~ 2^-48 ||A|| ||v||, far below
-            // what the first correction needs (its result is ~1e-14 off from the
-            // FP32 solve anyway); it is never used to accept a pair.
-            const cx<float> l0 = T.ld(k, k);
-            for (int i = 1; i <= n; ++i) {
-                const cx<float> vi = dx[i - 1];
-                float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f;
-                ff_mac(sr, er, -l0.r, vi.r);
-                ff_mac(sr, er, l0.i, vi.i);
-                ff_mac(si, ei, -l0.r, vi.i);
-                ff_mac(si, ei, -l0.i, vi.r);
-                for (int j = 1; j <= n; ++j) {
-                    const cx<float> ah = Ah.ld(i, j), al = Al.ld(i, j), vj = dx[j - 1];
-                    ff_mac(sr, er, ah.r, vj.r);
-                    ff_mac(sr, er, -ah.i, vj.i);
-                    ff_mac(si, ei, ah.r, vj.i);
-                    ff_mac(si, ei, ah.i, vj.r);
-                    er = fmaf(-al.i, vj.i, fmaf(al.r, vj.r, er));
-                    ei = fmaf(al.i, vj.r, fmaf(al.r, vj.i, ei));
+        n_res64 += step >= ff_steps;
+        n_ff += step < ff_steps;
+        if (step < ff_steps) {
+            // The first ff_steps residuals (1 or 2) in float-float on the FP32
+            // pipe (error ~ 2^-48 ||A|| ||v||); they drive the first corrections
+            // and never accept a pair.  With an FP32 Jacobian each Newton step
+            // gains a factor of about eps32 * cond, so most pairs reach the
+            // acceptance level after the second correction: with ff_steps = 2
+            // the one FP64 residual is usually the accepting one.  Step 0: v0 and
+            // lambda0 are FP32 numbers (dx holds v0); step 1: v and lambda split
+            // into FP32 heads (into dx, free until the next correction) and tails.
+            if (step == 0) {
+                ff_residual<MAXN, false>(n, Ah, Al, dx, vl, T.ld(k, k), mk(0.f, 0.f), r32);
+            } else {
+                for (int i = 0; i < n; ++i) {
+                    dx[i] = down(v[i]);
+                    vl[i] = down(csub(v[i], up(dx[i])));
                 }
-                r32[i - 1] = mk(__fadd_rn(sr, er), __fadd_rn(si, ei));
+                const cx<float> lh = down(lam);
+                ff_residual<MAXN, true>(n, Ah, Al, dx, vl, lh, down(csub(lam, up(lh))), r32);
             }
         } else {
             // FP64 residual: the one that accepts
@@ -630,7 +959,28 @@ int schur_group(int n)
     if (e && !strcmp(e, "warp")) return n <= 16 ? 16 : (n <= 32 ? 32 : 0);
     if (e && !strcmp(e, "warp16")) return n <= 16 ? 16 : 0;
     if (e && !strcmp(e, "warp32")) return n <= 32 ? 32 : 0;
+    if (e && !strcmp(e, "group4")) return n <= 16 ? 4 : 0;
+    if (e && !strcmp(e, "group8")) return n <= 16 ? 8 : 0;
+    if (n <= 16) return 8;
     return (n >= 24 && n <= 32) ? 32 : 0;
+}
+
+template <int G>
+long long group_schur_blocks(int n, long long N, int blocks_per_sm)
+{
+    cudaFuncSetAttribute(schur32_group_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)group_schur_smem(16, G));
+    const int sms = device_sms();
+    int per_sm = blocks_per_sm;
+    if (per_sm <= 0) {
+        per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, schur32_group_kernel<G>, kGroupSchurThreads,
+                                                      group_schur_smem(n, G));
+        if (per_sm < 1) per_sm = 1;
+    }
+    const long long per_block = kGroupSchurThreads / G;
+    const long long need = (N + per_block - 1) / per_block;
+    return std::max<long long>(1, std::min<long long>(need, (long long)sms * per_sm));
 }
 
 template <int G>
@@ -675,7 +1025,13 @@ cudaError_t launch_schur(const MixedArgs &a, int blocks_per_sm, cudaStream_t st)
     const long long cnt = a.m_end - a.m_begin;
     const MixedBufs b = mixed_bufs(a);
     const int G = schur_group(n);
-    if (G == 16)
+    if (G == 4)
+        schur32_group_kernel<4><<<(unsigned)group_schur_blocks<4>(n, cnt, blocks_per_sm), kGroupSchurThreads,
+                                  group_schur_smem(n, 4), st>>>(a, b.buf, b.flags);
+    else if (G == 8)
+        schur32_group_kernel<8><<<(unsigned)group_schur_blocks<8>(n, cnt, blocks_per_sm), kGroupSchurThreads,
+                                  group_schur_smem(n, 8), st>>>(a, b.buf, b.flags);
+    else if (G == 16)
         schur32_warp_kernel<16><<<(unsigned)warp_schur_blocks<16>(n, cnt, blocks_per_sm), kWarpSchurThreads,
                                   warp_schur_smem(n, 16), st>>>(a, b.buf, b.flags);
     else if (G == 32)
@@ -760,7 +1116,9 @@ cudaError_t launch_mixed_overlap(const MixedArgs &a0, cudaStream_t st, cudaStrea
     // FP32+refine eigensolves/s serial -> overlapped: n=8 36.1 -> 41.0 M/s,
     // n=16 5.10 -> 5.87 M/s, n=24 1.63 -> 1.72 M/s, n=32 0.726 -> 0.846 M/s);
     // VES_MIXED_OVERLAP_BLOCKS_PER_SM overrides
-    int bps = a.blocks_per_sm > 0 ? a.blocks_per_sm : (schur_group(a.g.n) ? 6 : 4);
+    // (the group kernel: as many as shared memory holds)
+    const int G = schur_group(a.g.n);
+    int bps = a.blocks_per_sm > 0 ? a.blocks_per_sm : (G == 4 || G == 8 ? 0 : (G ? 6 : 4));
     if (a.blocks_per_sm <= 0)
         if (const char *ev = getenv("VES_MIXED_OVERLAP_BLOCKS_PER_SM")) {
             const int v = atoi(ev);
@@ -821,6 +1179,8 @@ void load_mixed_kernels()
     load_kernel(refine_kernel<32, true>);
     load_kernel(schur32_warp_kernel<16>);
     load_kernel(refine_kernel<16, true>);
+    load_kernel(schur32_group_kernel<8>);
+    load_kernel(schur32_group_kernel<4>);
     load_kernel(dupcheck_kernel<false>);
     load_kernel(dupcheck_kernel<true>);
 }

@@ -89,6 +89,26 @@ cudaError_t launch_gemm_bf16(int M, int N, int K, const void *A, int lda, const 
     return cudaGetLastError();
 }
 
+// Split-K product for the weight gradients (K = the batch): S partial FP32
+// products part[z] = A[:, Kz] * B[Kz, :] (z-th K range), M x N each with
+// leading dimension ldc, one after the other; the caller sums them.
+cudaError_t launch_gemm_bf16_splitk(int M, int N, int K, const void *A, int lda, const void *Bt, int ldb, float *part,
+                                    int ldc, int S, int *err, cudaStream_t st)
+{
+    if (M <= 0 || N <= 0 || K <= 0 || S < 1) return cudaSuccess;
+    const auto *a = static_cast<const __nv_bfloat16 *>(A);
+    const auto *b = static_cast<const __nv_bfloat16 *>(Bt);
+    const unsigned gx = (unsigned)((M + tc::kM - 1) / tc::kM);
+    const long long zs = (long long)M * ldc;
+    if (N > 64)
+        tc::gemm_bf16_kernel<256><<<dim3(gx, (N + 255) / 256, S), 128, 0, st>>>(a, lda, b, ldb, M, N, K, nullptr, 0,
+                                                                                nullptr, part, ldc, err, zs);
+    else
+        tc::gemm_bf16_kernel<64><<<dim3(gx, (N + 63) / 64, S), 128, 0, st>>>(a, lda, b, ldb, M, N, K, nullptr, 0,
+                                                                              nullptr, part, ldc, err, zs);
+    return cudaGetLastError();
+}
+
 namespace {
 
 constexpr int kMaxDimNet = 64;
@@ -101,11 +121,13 @@ __device__ __forceinline__ long long soa_off_s(long long m, long long len, int t
 }
 
 constexpr int kMaxFourier = 64;  // n_params * fourier
-constexpr int kMaxFeat = 64 + 2 * kMaxFourier + 2 * kMaxDimNet;
+constexpr int kMaxFeat = 64 + 2 * kMaxFourier + 3 * kMaxDimNet;
 
-// raw (unnormalised) features of matrix m into f[0 .. P + 2PF + 2n):
-// parameters, sin / cos ((pi/2) k p) for k = 1..F, Re diag A, Im diag A
-__device__ __forceinline__ void raw_features(long long m, int n, int P, int F, int tc, const double *params,
+// raw (unnormalised) features of matrix m into f[0 .. P + 2PF + 2n + S(n-1)):
+// parameters, sin / cos ((pi/2) k p) for k = 1..F, Re diag A, Im diag A, and
+// with S = 1 the 2-norms of the n - 1 subdiagonals of A (how far A is from
+// upper triangular, diagonal by diagonal)
+__device__ __forceinline__ void raw_features(long long m, int n, int P, int F, int S, int tc, const double *params,
                                              const double *rA, const double *iA, float *f)
 {
     for (int q = 0; q < P; ++q) {
@@ -125,10 +147,20 @@ __device__ __forceinline__ void raw_features(long long m, int n, int P, int F, i
         f[o + i] = (float)rA[k];
         f[o + n + i] = (float)iA[k];
     }
+    if (S) {
+        for (int d = 1; d < n; ++d) {  // subdiagonal d: elements (i + d, i)
+            double s2 = 0.0;
+            for (int i = 0; i + d < n; ++i) {
+                const long long k = mo + (long long)(i + d + i * n) * tc;
+                s2 = fma(rA[k], rA[k], fma(iA[k], iA[k], s2));
+            }
+            f[o + 2 * n + d - 1] = (float)sqrt(s2);
+        }
+    }
 }
 
 // features -> standardised BF16 rows [count x kin_pad]
-__global__ void features_kernel(long long count, int n, int P, int F, int tc, const double *params, const double *rA,
+__global__ void features_kernel(long long count, int n, int P, int F, int S, int tc, const double *params, const double *rA,
                                 const double *iA, const float *mean, const float *stdv, int kin, int kin_pad, bf16 *X,
                                 const int *rows)
 {
@@ -136,7 +168,7 @@ __global__ void features_kernel(long long count, int n, int P, int F, int tc, co
     if (r >= count) return;
     const long long m = rows ? rows[r] : r;
     float f[kMaxFeat];
-    raw_features(m, n, P, F, tc, params, rA, iA, f);
+    raw_features(m, n, P, F, S, tc, params, rA, iA, f);
     for (int c = 0; c < kin_pad; ++c) {
         float v = 0.f;
         if (c < kin) v = mean ? (f[c] - mean[c]) / stdv[c] : f[c];
@@ -381,6 +413,46 @@ __global__ void dh_kernel(int B, int out, int in, const float *dZ, const float *
     dH[(long long)b * in + i] = acc;
 }
 
+// out[c][r] = in[r][c] as BF16 (in: R x C row-major, leading dimension ldi;
+// out: C x R, leading dimension ldo), through 32 x 32 shared-memory tiles;
+// block (32, 8).  Makes the K-major operands of the backward GEMMs, whose K is
+// the batch.
+template <class T>
+__global__ void transpose_bf16_kernel(int R, int C, const T *in, int ldi, bf16 *out, int ldo)
+{
+    __shared__ float tile[32][33];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int r = r0 + y, c = c0 + threadIdx.x;
+        tile[y][threadIdx.x] = (r < R && c < C) ? to_f32(in[(long long)r * ldi + c]) : 0.f;
+    }
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int c = c0 + y, r = r0 + threadIdx.x;
+        if (c < C && r < R) out[(long long)c * ldo + r] = __float2bfloat16(tile[threadIdx.x][y]);
+    }
+}
+
+// out[e] = sum_z part[z * zs + e]: the partial products of a split-K GEMM
+__global__ void sum_splits_kernel(long long n, int S, long long zs, const float *part, float *out)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    float acc = 0.f;
+    for (int z = 0; z < S; ++z) acc += part[z * zs + e];
+    out[e] = acc;
+}
+
+// db[o] = sum_b dZ[b][o]
+__global__ void colsum_kernel(int B, int out, const float *dZ, float *db)
+{
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= out) return;
+    float acc = 0.f;
+    for (int b = 0; b < B; ++b) acc += dZ[(long long)b * out + o];
+    db[o] = acc;
+}
+
 __global__ void adam_kernel(long long n, float *p, const float *g, float *m, float *v, float lr, float b1, float b2,
                             float eps, float c1, float c2, bf16 *pb)
 {
@@ -434,7 +506,10 @@ void load_shiftnet_kernels()
     load_kernel(chamfer_kernel);
     load_kernel(gelu_bwd_kernel);
     load_kernel(dw_kernel<float>);
-    load_kernel(dw_kernel<bf16>);
+    load_kernel(transpose_bf16_kernel<float>);
+    load_kernel(transpose_bf16_kernel<bf16>);
+    load_kernel(sum_splits_kernel);
+    load_kernel(colsum_kernel);
     load_kernel(gelu_f32_kernel);
     load_kernel(dense_out_kernel);
     load_kernel(dh_kernel);
@@ -450,7 +525,7 @@ void load_shiftnet_kernels()
 // ---------------------------------------------------------------------------
 struct ves_shiftnet {
     ves_shiftnet_config cfg{};
-    int n = 0, P = 0, H = 0, L = 0, F = 0, kin = 0, kin_pad = 0, nout = 0, nout_pad = 0;
+    int n = 0, P = 0, H = 0, L = 0, F = 0, S = 0, kin = 0, kin_pad = 0, nout = 0, nout_pad = 0;
     // layers 0..L-1: hidden (tcgen05, BF16 in, FP32 accumulate, GELU);
     // layer L: output (FP32, CUDA cores)
     int in[ves::kMaxLayers + 1] = {}, out[ves::kMaxLayers + 1] = {};
@@ -503,14 +578,14 @@ bool config_ok(const ves_shiftnet_config &c)
     return c.dim >= 1 && c.dim <= ves::kMaxDimNet && c.n_params >= 0 && c.n_params <= 64 && c.hidden >= 16 &&
            c.hidden <= 256 && (c.hidden % 16) == 0 && c.layers >= 1 && c.layers <= ves::kMaxLayers &&
            c.fourier >= 0 && c.n_params * c.fourier <= ves::kMaxFourier && (c.loss == 0 || c.loss == 1) &&
-           c.delta > 0.f && c.delta < 1e3f;
+           c.delta > 0.f && c.delta < 1e3f && (c.subdiag == 0 || c.subdiag == 1);
 }
 
 void set_geometry(ves_shiftnet *t, const ves_shiftnet_config &c)
 {
     t->cfg = c;
-    t->n = c.dim; t->P = c.n_params; t->H = c.hidden; t->L = c.layers; t->F = c.fourier;
-    t->kin = t->P + 2 * t->P * t->F + 2 * t->n;
+    t->n = c.dim; t->P = c.n_params; t->H = c.hidden; t->L = c.layers; t->F = c.fourier; t->S = c.subdiag ? 1 : 0;
+    t->kin = t->P + 2 * t->P * t->F + 2 * t->n + t->S * (t->n - 1);
     t->kin_pad = (t->kin + 31) / 32 * 32;
     t->nout = 2 * t->n;
     t->nout_pad = (t->nout + 15) / 16 * 16;
@@ -612,6 +687,89 @@ int create_from_config(ves_shiftnet **out, const ves_shiftnet_config &c)
     return VES_OK;
 }
 
+// Gradient buffers of one training step over `batch` rows.
+struct GradBufs {
+    float *gW[ves::kMaxLayers + 1] = {}, *gb[ves::kMaxLayers + 1] = {};
+    float *dA = nullptr, *dB = nullptr;  // FP32 [batch x max(H, nout_pad)]: dY, then dH / dZ of the hidden layers
+    ves::bf16 *dZ16 = nullptr;            // dZ as BF16 [batch x H]: A operand of dH = dZ W
+    ves::bf16 *dZt = nullptr;             // dZ transposed [H x batch]: A operand of dW = dZ^T Hin
+    ves::bf16 *HinT = nullptr;            // the layer input transposed [max(kin_pad, H) x batch]
+    ves::bf16 *WbT = nullptr;             // BF16 weights transposed [H x H]: B operand of dH
+    float *part = nullptr;                // split-K partials [splits x H x max(kin_pad, H)]
+    int splits = 1;
+};
+
+// split-K factor of the weight-gradient GEMMs: K = batch in ranges of >= 64
+int grad_splits(int batch) { return std::max(1, std::min(16, batch / 64)); }
+
+bool grad_alloc(const ves_shiftnet *t, int batch, GradBufs &g)
+{
+    const int H = t->H, wmax = std::max(H, t->nout_pad), imax = std::max(t->kin_pad, H);
+    g.splits = grad_splits(batch);
+    bool ok = cudaMalloc(&g.dA, (size_t)batch * wmax * 4) == cudaSuccess &&
+              cudaMalloc(&g.dB, (size_t)batch * wmax * 4) == cudaSuccess &&
+              cudaMalloc(&g.dZ16, (size_t)batch * H * 2) == cudaSuccess &&
+              cudaMalloc(&g.dZt, (size_t)batch * H * 2) == cudaSuccess &&
+              cudaMalloc(&g.HinT, (size_t)batch * imax * 2) == cudaSuccess &&
+              cudaMalloc(&g.WbT, (size_t)H * H * 2) == cudaSuccess &&
+              cudaMalloc(&g.part, (size_t)g.splits * H * imax * 4) == cudaSuccess;
+    for (int l = 0; l <= t->L && ok; ++l) {
+        ok &= cudaMalloc(&g.gW[l], (size_t)t->out[l] * t->in[l] * 4) == cudaSuccess;
+        ok &= cudaMalloc(&g.gb[l], (size_t)t->out[l] * 4) == cudaSuccess;
+    }
+    return ok;
+}
+
+void grad_free(const ves_shiftnet *t, GradBufs &g)
+{
+    cudaFree(g.dA); cudaFree(g.dB); cudaFree(g.dZ16); cudaFree(g.dZt); cudaFree(g.HinT); cudaFree(g.WbT);
+    cudaFree(g.part);
+    for (int l = 0; l <= t->L; ++l) { cudaFree(g.gW[l]); cudaFree(g.gb[l]); }
+}
+
+// Loss and parameter gradients of one batch (features Xb, standardised
+// targets Tb), into g.gW / g.gb; the batch loss is added to *loss.
+//   output layer (FP32 on CUDA cores, like its forward): dW = dY^T Hf, dH = dY W
+//   hidden layers (tcgen05): dW = dZ^T Hin as a split-K BF16 GEMM over the
+//   batch (FP32 partials summed), dH = dZ W as a BF16 GEMM with W transposed;
+//   db = column sums of dZ; then dZ of the layer below = dH * GELU'(Z).
+// dZ is rounded to BF16 for the tensor cores and accumulated in FP32.
+void step_gradients(const ves_shiftnet *t, int batch, const ves::bf16 *Xb, const float *Tb, const Acts &a,
+                    GradBufs &g, float *loss, int *err, cudaStream_t st)
+{
+    const int n = t->n, H = t->H, L = t->L;
+    forward(t, batch, Xb, a, err, st, true);
+    ves::chamfer_kernel<<<ves::nb(batch, 128), 128, 0, st>>>(batch, n, t->nout_pad, a.Y, Tb, g.dA, loss, t->cfg.loss,
+                                                             t->cfg.delta);
+    ves::dw_kernel<float><<<dim3(ves::nb(H, 128), t->nout_pad), 128, 0, st>>>(batch, t->nout_pad, H, g.dA, a.Hf, H,
+                                                                             g.gW[L], g.gb[L]);
+    ves::dh_kernel<<<dim3(ves::nb(H, 128), batch), 128, 0, st>>>(batch, t->nout_pad, H, g.dA, t->W[L], g.dB);
+    ves::gelu_bwd_kernel<<<ves::nb((long long)batch * H), 256, 0, st>>>((long long)batch * H, g.dB, a.Z[L - 1], g.dB);
+    float *dZ = g.dB, *dH = g.dA;
+    const dim3 tb(32, 8);
+    for (int l = L - 1; l >= 0; --l) {
+        const ves::bf16 *Hin = l == 0 ? Xb : a.Hs[l - 1];
+        const int in = t->in[l];  // kin_pad for the first layer, H otherwise (= the leading dimension of Hin)
+        const long long nz = (long long)batch * H;
+        ves::transpose_bf16_kernel<float><<<dim3(ves::nb(H, 32), ves::nb(batch, 32)), tb, 0, st>>>(batch, H, dZ, H,
+                                                                                                  g.dZt, batch);
+        ves::transpose_bf16_kernel<ves::bf16><<<dim3(ves::nb(in, 32), ves::nb(batch, 32)), tb, 0, st>>>(
+            batch, in, Hin, in, g.HinT, batch);
+        ves::launch_gemm_bf16_splitk(H, in, batch, g.dZt, batch, g.HinT, batch, g.part, in, g.splits, err, st);
+        ves::sum_splits_kernel<<<ves::nb((long long)H * in), 256, 0, st>>>((long long)H * in, g.splits,
+                                                                          (long long)H * in, g.part, g.gW[l]);
+        ves::colsum_kernel<<<ves::nb(H, 128), 128, 0, st>>>(batch, H, dZ, g.gb[l]);
+        if (l > 0) {
+            ves::to_bf16_kernel<<<ves::nb(nz), 256, 0, st>>>(nz, dZ, g.dZ16);
+            ves::transpose_bf16_kernel<ves::bf16><<<dim3(ves::nb(H, 32), ves::nb(H, 32)), tb, 0, st>>>(
+                H, H, t->Wb[l], H, g.WbT, H);
+            ves::launch_gemm_bf16(batch, H, H, g.dZ16, H, g.WbT, H, nullptr, 0, nullptr, dH, H, err, st);
+            ves::gelu_bwd_kernel<<<ves::nb(nz), 256, 0, st>>>(nz, dH, a.Z[l - 1], dH);
+            float *tmp = dZ; dZ = dH; dH = tmp;
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -627,6 +785,7 @@ void ves_shiftnet_default_config(ves_shiftnet_config *c)
     c->loss = VES_SHIFTNET_LOSS_CHAMFER;
     c->delta = 0.01f;
     c->seed = 0;
+    c->subdiag = 0;
 }
 
 int ves_shiftnet_create_config(ves_shiftnet **out, const ves_shiftnet_config *cfg)
@@ -663,36 +822,30 @@ int ves_shiftnet_train(ves_shiftnet *t, long long count, int thread_cnt, const d
     if (t->P > 0 && !params) return fail(VES_ERR_ARG, "shiftnet train: the network needs family parameters");
     ves::set_error_message("");
     cudaStream_t st = (cudaStream_t)stream;
-    const int n = t->n, H = t->H, L = t->L;
+    const int n = t->n, L = t->L;
     ves::bf16 *Xall = nullptr, *Xb = nullptr;
-    float *Tall = nullptr, *Tb = nullptr, *dA = nullptr, *dB = nullptr, *loss = nullptr;
-    float *gW[ves::kMaxLayers + 1] = {}, *gb[ves::kMaxLayers + 1] = {};
+    float *Tall = nullptr, *Tb = nullptr, *loss = nullptr;
+    GradBufs g;
     int *rows = nullptr, *err = nullptr;
     char *actbuf = nullptr;
-    const int wmax = std::max(H, t->nout_pad);
     bool ok = cudaMalloc(&Xall, (size_t)count * t->kin_pad * 2) == cudaSuccess &&
               cudaMalloc(&Tall, (size_t)count * t->nout_pad * 4) == cudaSuccess &&
               cudaMalloc(&Xb, (size_t)batch * t->kin_pad * 2) == cudaSuccess &&
               cudaMalloc(&Tb, (size_t)batch * t->nout_pad * 4) == cudaSuccess &&
-              cudaMalloc(&dA, (size_t)batch * wmax * 4) == cudaSuccess &&
-              cudaMalloc(&dB, (size_t)batch * wmax * 4) == cudaSuccess &&
               cudaMalloc(&loss, 4 * 2) == cudaSuccess && cudaMalloc(&rows, (size_t)count * 4) == cudaSuccess &&
-              cudaMalloc(&err, 4) == cudaSuccess && cudaMalloc(&actbuf, acts_bytes(t, batch)) == cudaSuccess;
-    for (int l = 0; l <= L && ok; ++l) {
-        ok &= cudaMalloc(&gW[l], (size_t)t->out[l] * t->in[l] * 4) == cudaSuccess;
-        ok &= cudaMalloc(&gb[l], (size_t)t->out[l] * 4) == cudaSuccess;
-    }
+              cudaMalloc(&err, 4) == cudaSuccess && cudaMalloc(&actbuf, acts_bytes(t, batch)) == cudaSuccess &&
+              grad_alloc(t, batch, g);
     int rc = ok ? VES_OK : VES_ERR_NOMEM;
     if (rc == VES_OK) {
         char *w = actbuf;
         const Acts a = carve_acts(t, batch, w);
         cudaMemsetAsync(err, 0, 4, st);
         // standardisation statistics over the whole training set
-        ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, t->P, t->F, thread_cnt, params, rA, iA,
+        ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, t->P, t->F, t->S, thread_cnt, params, rA, iA,
                                                              nullptr, nullptr, t->kin, t->kin_pad, Xall, nullptr);
         ves::colstats_bf16_kernel<<<ves::nb(t->kin_pad), 256, 0, st>>>(count, t->kin_pad, t->kin_pad, Xall, t->fmean,
                                                                       t->fstd);
-        ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, t->P, t->F, thread_cnt, params, rA, iA,
+        ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, t->P, t->F, t->S, thread_cnt, params, rA, iA,
                                                              t->fmean, t->fstd, t->kin, t->kin_pad, Xall, nullptr);
         ves::targets_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, thread_cnt, rE, iE, nullptr, nullptr,
                                                             t->nout_pad, Tall, nullptr);
@@ -712,42 +865,21 @@ int ves_shiftnet_train(ves_shiftnet *t, long long count, int thread_cnt, const d
             cudaMemsetAsync(loss, 0, 4, st);
             for (long long s = 0; s < steps_per_epoch; ++s) {
                 const int *r = rows + s * batch;
-                ves::features_kernel<<<ves::nb(batch), 256, 0, st>>>(batch, n, t->P, t->F, thread_cnt, params, rA,
-                                                                     iA, t->fmean, t->fstd, t->kin, t->kin_pad, Xb, r);
+                ves::features_kernel<<<ves::nb(batch), 256, 0, st>>>(batch, n, t->P, t->F, t->S, thread_cnt, params,
+                                                                     rA, iA, t->fmean, t->fstd, t->kin, t->kin_pad,
+                                                                     Xb, r);
                 ves::targets_kernel<<<ves::nb(batch), 256, 0, st>>>(batch, n, thread_cnt, rE, iE, t->tmean, t->tstd,
                                                                     t->nout_pad, Tb, r);
-                forward(t, batch, Xb, a, err, st, true);
-                ves::chamfer_kernel<<<ves::nb(batch, 128), 128, 0, st>>>(batch, n, t->nout_pad, a.Y, Tb, dA, loss,
-                                                                         t->cfg.loss, t->cfg.delta);
-                // output layer (FP32): dW = dY^T Hf, dH = dY W, then through GELU
-                ves::dw_kernel<float><<<dim3(ves::nb(H, 128), t->nout_pad), 128, 0, st>>>(
-                    batch, t->nout_pad, H, dA, a.Hf, H, gW[L], gb[L]);
-                ves::dh_kernel<<<dim3(ves::nb(H, 128), batch), 128, 0, st>>>(batch, t->nout_pad, H, dA, t->W[L], dB);
-                ves::gelu_bwd_kernel<<<ves::nb((long long)batch * H), 256, 0, st>>>((long long)batch * H, dB,
-                                                                                    a.Z[L - 1], dB);
-                // hidden layers L-1 .. 0; dZ holds the gradient of the current layer's pre-activation
-                float *dZ = dB, *dH = dA;
-                for (int l = L - 1; l >= 0; --l) {
-                    const ves::bf16 *Hin = l == 0 ? Xb : a.Hs[l - 1];
-                    const int ldh = l == 0 ? t->kin_pad : H;
-                    ves::dw_kernel<ves::bf16><<<dim3(ves::nb(t->in[l], 128), H), 128, 0, st>>>(
-                        batch, H, t->in[l], dZ, Hin, ldh, gW[l], gb[l]);
-                    if (l > 0) {
-                        ves::dh_kernel<<<dim3(ves::nb(H, 128), batch), 128, 0, st>>>(batch, H, H, dZ, t->W[l], dH);
-                        ves::gelu_bwd_kernel<<<ves::nb((long long)batch * H), 256, 0, st>>>((long long)batch * H, dH,
-                                                                                            a.Z[l - 1], dH);
-                        float *tmp = dZ; dZ = dH; dH = tmp;
-                    }
-                }
+                step_gradients(t, batch, Xb, Tb, a, g, loss, err, st);
                 ++t->step;
                 const float lr_k = (float)(lr * (0.02 + 0.49 * (1.0 + std::cos(3.141592653589793 * (double)k++ /
                                                                                  total_steps))));
                 const float c1 = 1.f - std::pow(b1, (float)t->step), c2 = 1.f - std::pow(b2, (float)t->step);
                 for (int l = 0; l <= L; ++l) {
                     const long long nw = (long long)t->out[l] * t->in[l];
-                    ves::adam_kernel<<<ves::nb(nw), 256, 0, st>>>(nw, t->W[l], gW[l], t->mW[l], t->vW[l], lr_k, b1, b2,
-                                                                 eps, c1, c2, l < L ? t->Wb[l] : nullptr);
-                    ves::adam_kernel<<<ves::nb(t->out[l]), 256, 0, st>>>(t->out[l], t->b[l], gb[l], t->mb[l],
+                    ves::adam_kernel<<<ves::nb(nw), 256, 0, st>>>(nw, t->W[l], g.gW[l], t->mW[l], t->vW[l], lr_k, b1,
+                                                                 b2, eps, c1, c2, l < L ? t->Wb[l] : nullptr);
+                    ves::adam_kernel<<<ves::nb(t->out[l]), 256, 0, st>>>(t->out[l], t->b[l], g.gb[l], t->mb[l],
                                                                         t->vb[l], lr_k, b1, b2, eps, c1, c2, nullptr);
                 }
             }
@@ -761,11 +893,68 @@ int ves_shiftnet_train(ves_shiftnet *t, long long count, int thread_cnt, const d
         if (he) rc = VES_ERR_CUDA;
         if (cudaDeviceSynchronize() != cudaSuccess) rc = VES_ERR_CUDA;
     }
-    cudaFree(Xall); cudaFree(Tall); cudaFree(Xb); cudaFree(Tb); cudaFree(dA); cudaFree(dB); cudaFree(loss);
+    cudaFree(Xall); cudaFree(Tall); cudaFree(Xb); cudaFree(Tb); cudaFree(loss);
     cudaFree(rows); cudaFree(err); cudaFree(actbuf);
-    for (int l = 0; l <= L; ++l) { cudaFree(gW[l]); cudaFree(gb[l]); }
+    grad_free(t, g);
     if (rc == VES_ERR_NOMEM) return fail(rc, "shiftnet train: device allocation failed");
     if (rc != VES_OK) return fail(rc, "shiftnet train: a kernel failed or a tensor-core wait timed out");
+    return rc;
+}
+
+size_t ves_shiftnet_param_count(const ves_shiftnet *t)
+{
+    if (!t) return 0;
+    size_t c = 0;
+    for (int l = 0; l <= t->L; ++l) c += (size_t)t->out[l] * t->in[l] + t->out[l];
+    return c;
+}
+
+int ves_shiftnet_gradient(const ves_shiftnet *t, long long count, int thread_cnt, const double *params,
+                          const double *rA, const double *iA, const double *rE, const double *iE, float *grad,
+                          float *loss, void *stream)
+{
+    if (!t || count < 32 || count > 65536 || thread_cnt < 1 || (count % thread_cnt) || !rA || !iA || !rE || !iE ||
+        !grad || !loss)
+        return fail(VES_ERR_ARG, "shiftnet gradient: bad arguments (32 <= count <= 65536, a multiple of thread_cnt)");
+    if (t->P > 0 && !params) return fail(VES_ERR_ARG, "shiftnet gradient: the network needs family parameters");
+    ves::set_error_message("");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int batch = (int)count;
+    ves::bf16 *X = nullptr;
+    float *T = nullptr;
+    int *err = nullptr;
+    char *actbuf = nullptr;
+    GradBufs g;
+    bool ok = cudaMalloc(&X, (size_t)batch * t->kin_pad * 2) == cudaSuccess &&
+              cudaMalloc(&T, (size_t)batch * t->nout_pad * 4) == cudaSuccess && cudaMalloc(&err, 4) == cudaSuccess &&
+              cudaMalloc(&actbuf, acts_bytes(t, batch)) == cudaSuccess && grad_alloc(t, batch, g);
+    int rc = ok ? VES_OK : VES_ERR_NOMEM;
+    if (rc == VES_OK) {
+        char *w = actbuf;
+        const Acts a = carve_acts(t, batch, w);
+        cudaMemsetAsync(err, 0, 4, st);
+        cudaMemsetAsync(loss, 0, 4, st);
+        ves::features_kernel<<<ves::nb(batch), 256, 0, st>>>(batch, t->n, t->P, t->F, t->S, thread_cnt, params, rA, iA,
+                                                             t->fmean, t->fstd, t->kin, t->kin_pad, X, nullptr);
+        ves::targets_kernel<<<ves::nb(batch), 256, 0, st>>>(batch, t->n, thread_cnt, rE, iE, t->tmean, t->tstd,
+                                                            t->nout_pad, T, nullptr);
+        step_gradients(t, batch, X, T, a, g, loss, err, st);
+        size_t off = 0;
+        for (int l = 0; l <= t->L; ++l) {
+            const size_t nw = (size_t)t->out[l] * t->in[l];
+            cudaMemcpyAsync(grad + off, g.gW[l], nw * 4, cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(grad + off + nw, g.gb[l], t->out[l] * 4, cudaMemcpyDeviceToDevice, st);
+            off += nw + t->out[l];
+        }
+        int he = 0;
+        if (cudaStreamSynchronize(st) != cudaSuccess) rc = VES_ERR_CUDA;
+        cudaMemcpy(&he, err, 4, cudaMemcpyDeviceToHost);
+        if (he) rc = VES_ERR_CUDA;
+    }
+    cudaFree(X); cudaFree(T); cudaFree(err); cudaFree(actbuf);
+    grad_free(t, g);
+    if (rc == VES_ERR_NOMEM) return fail(rc, "shiftnet gradient: device allocation failed");
+    if (rc != VES_OK) return fail(rc, "shiftnet gradient: a kernel failed or a tensor-core wait timed out");
     return rc;
 }
 
@@ -794,7 +983,7 @@ int ves_shiftnet_predict(const ves_shiftnet *t, long long count, int thread_cnt,
     w += ((size_t)count * t->kin_pad * 2 + 255) & ~(size_t)255;
     const Acts a = carve_acts(t, (size_t)count, w);
     int *err = nullptr;  // a GEMM wait that gives up leaves its tile unwritten; training checks the flag
-    ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, t->n, t->P, t->F, thread_cnt, params, rA, iA,
+    ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, t->n, t->P, t->F, t->S, thread_cnt, params, rA, iA,
                                                          t->fmean, t->fstd, t->kin, t->kin_pad, X, nullptr);
     if (forward(t, (int)count, X, a, err, st, false) != cudaSuccess) return fail(VES_ERR_CUDA, "shiftnet predict: launch failed");
     ves::shifts_out_kernel<<<ves::nb(count), 256, 0, st>>>(count, t->n, thread_cnt, t->nout_pad, a.Y, t->tmean,
@@ -810,7 +999,7 @@ int ves_shiftnet_save(const ves_shiftnet *t, const char *path)
     if (!t || !path) return fail(VES_ERR_ARG, "shiftnet save: null argument");
     FILE *f = fopen(path, "wb");
     if (!f) return fail(VES_ERR_ARG, "shiftnet save: cannot open the file");
-    const int hdr[9] = {0x56455353, 2, t->n, t->P, t->H, t->L, t->F, t->cfg.loss, (int)t->step};
+    const int hdr[10] = {0x56455353, 3, t->n, t->P, t->H, t->L, t->F, t->cfg.loss, (int)t->step, t->S};
     bool ok = fwrite(hdr, sizeof hdr, 1, f) == 1 && fwrite(&t->cfg.delta, 4, 1, f) == 1 &&
               fwrite(&t->cfg.seed, 8, 1, f) == 1;
     auto put = [&](const float *d, size_t cnt) {
@@ -832,15 +1021,18 @@ int ves_shiftnet_load(ves_shiftnet **out, const char *path)
     if (!out || !path) return fail(VES_ERR_ARG, "shiftnet load: null argument");
     FILE *f = fopen(path, "rb");
     if (!f) return fail(VES_ERR_ARG, "shiftnet load: cannot open the file");
-    int hdr[9];
+    // version 2: 9 header ints; version 3 adds the subdiagonal-feature flag
+    int hdr[10] = {};
     ves_shiftnet_config c;
     ves_shiftnet_default_config(&c);
-    if (fread(hdr, sizeof hdr, 1, f) != 1 || hdr[0] != 0x56455353 || hdr[1] != 2 || fread(&c.delta, 4, 1, f) != 1 ||
-        fread(&c.seed, 8, 1, f) != 1) {
+    bool hok = fread(hdr, sizeof(int), 9, f) == 9 && hdr[0] == 0x56455353 && (hdr[1] == 2 || hdr[1] == 3);
+    if (hok && hdr[1] == 3) hok = fread(hdr + 9, sizeof(int), 1, f) == 1;
+    if (!hok || fread(&c.delta, 4, 1, f) != 1 || fread(&c.seed, 8, 1, f) != 1) {
         fclose(f);
-        return fail(VES_ERR_ARG, "shiftnet load: not a version-2 shift network checkpoint");
+        return fail(VES_ERR_ARG, "shiftnet load: not a version-2 or version-3 shift network checkpoint");
     }
     c.dim = hdr[2]; c.n_params = hdr[3]; c.hidden = hdr[4]; c.layers = hdr[5]; c.fourier = hdr[6]; c.loss = hdr[7];
+    c.subdiag = hdr[9];
     ves_shiftnet *t = nullptr;
     int rc = create_from_config(&t, c);
     if (rc != VES_OK) { fclose(f); return rc; }

@@ -116,10 +116,16 @@ __device__ __forceinline__ float gelu(float x)
 }
 
 // NT: columns per CTA (16..256, multiple of 16).  grid = (ceil(M/128), ceil(N/NT)).
+//
+// Split K (gridDim.z > 1, the weight gradients of training, where K is the
+// batch): CTA z takes the K range [z * kz, (z + 1) * kz), kz a multiple of 32,
+// and writes its FP32 partial product to Cf + z * zstride (no bias, no C);
+// the caller sums the partials.
 template <int NT>
 __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *Bt,
                                                         int ldb, int M, int N, int K, const float *bias, int act,
-                                                        __nv_bfloat16 *C, float *Cf, int ldc, int *err)
+                                                        __nv_bfloat16 *C, float *Cf, int ldc, int *err,
+                                                        long long zstride = 0)
 {
     static_assert(NT % 16 == 0 && NT >= 16 && NT <= 256, "N tile");
     constexpr int kCols = NT <= 32 ? 32 : (NT <= 64 ? 64 : (NT <= 128 ? 128 : 256));  // TMEM columns
@@ -149,21 +155,29 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *A, 
     constexpr uint32_t idesc = make_idesc(kM, NT);
 
     unsigned phase = 0;
-    const int nchunks = (K + kKC - 1) / kKC;
+    // this CTA's K range (the whole of K unless split)
+    const int kz = gridDim.z > 1 ? (K + (int)gridDim.z * kKC - 1) / ((int)gridDim.z * kKC) * kKC : K;
+    const int kb = (int)blockIdx.z * kz, ke = min(K, kb + kz);
+    if (gridDim.z > 1) {
+        Cf += (long long)blockIdx.z * zstride;
+        bias = nullptr;
+        C = nullptr;
+    }
+    const int nchunks = ke > kb ? (ke - kb + kKC - 1) / kKC : 0;
     for (int c = 0; c < nchunks && !failed; ++c) {
-        const int k0 = c * kKC;
+        const int k0 = kb + c * kKC;
         // stage A: 128 rows x 8 core columns of 16 bytes
         constexpr int kcs = kKC / 8;  // core-matrix columns per chunk
         for (int p = tid; p < kM * kcs; p += 128) {
             const int r = p / kcs, kc = p % kcs, k = k0 + kc * 8;
             uint4 v = make_uint4(0, 0, 0, 0);
-            if (m0 + r < M && k < K) v = *reinterpret_cast<const uint4 *>(A + (size_t)(m0 + r) * lda + k);
+            if (m0 + r < M && k < ke) v = *reinterpret_cast<const uint4 *>(A + (size_t)(m0 + r) * lda + k);
             *reinterpret_cast<uint4 *>(sA + ((r >> 3) * kcs + kc) * 128 + (r & 7) * 16) = v;
         }
         for (int p = tid; p < NT * kcs; p += 128) {
             const int r = p / kcs, kc = p % kcs, k = k0 + kc * 8;
             uint4 v = make_uint4(0, 0, 0, 0);
-            if (n0 + r < N && k < K) v = *reinterpret_cast<const uint4 *>(Bt + (size_t)(n0 + r) * ldb + k);
+            if (n0 + r < N && k < ke) v = *reinterpret_cast<const uint4 *>(Bt + (size_t)(n0 + r) * ldb + k);
             *reinterpret_cast<uint4 *>(sB + ((r >> 3) * kcs + kc) * 128 + (r & 7) * 16) = v;
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // smem writes -> tensor core (async proxy)
@@ -190,6 +204,8 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *A, 
         for (int cb = 0; cb < NT; cb += 16) {
             float v[16];
             tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb, v);
+            if (nchunks == 0)  // an empty K range (split K): nothing was accumulated
+                for (int i = 0; i < 16; ++i) v[i] = 0.f;
             if (row < M) {
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {

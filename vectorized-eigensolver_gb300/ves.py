@@ -36,7 +36,7 @@ class VesError(RuntimeError):
 
 class ShiftNetConfig(ctypes.Structure):
     _fields_ = [("dim", _int), ("n_params", _int), ("hidden", _int), ("layers", _int), ("fourier", _int),
-                ("loss", _int), ("delta", ctypes.c_float), ("seed", ctypes.c_ulonglong)]
+                ("loss", _int), ("delta", ctypes.c_float), ("seed", ctypes.c_ulonglong), ("subdiag", _int)]
 
 
 VES_SHIFTNET_LOSS_CHAMFER, VES_SHIFTNET_LOSS_ROBUST = 0, 1
@@ -96,6 +96,8 @@ SIGNATURES = {
     "ves_shiftnet_train": (_int, [_VP, ctypes.c_longlong, _int, _VP, _VP, _VP, _VP, _VP, _int, _int,
                                   ctypes.c_float, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_float), _VP]),
     "ves_shiftnet_predict_workspace_size": (_size, [_VP, ctypes.c_longlong]),
+    "ves_shiftnet_param_count": (_size, [_VP]),
+    "ves_shiftnet_gradient": (_int, [_VP, ctypes.c_longlong, _int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "ves_shiftnet_predict": (_int, [_VP, ctypes.c_longlong, _int, _VP, _VP, _VP, _VP, _VP, _VP, _size, _VP]),
     "ves_shiftnet_save": (_int, [_VP, ctypes.c_char_p]),
     "ves_shiftnet_load": (_int, [ctypes.POINTER(_VP), ctypes.c_char_p]),
@@ -107,6 +109,7 @@ SIGNATURES = {
     "ves_soa_vec_from_complex": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP]),
     "ves_complex_from_soa_vec": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP]),
     "ves_eigensolve_noalloc": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "ves_partition_blocks": (_int, [_int, _int, _int, ctypes.POINTER(_int), ctypes.POINTER(_int)]),
     "ves_last_error": (ctypes.c_char_p, []),
     "ves_release": (None, []),
     "ves_version": (_int, []),
@@ -427,6 +430,17 @@ class ShiftNet:
                "ves_shiftnet_train")
         return list(losses)[:epochs]
 
+    def gradient(self, count, thread_cnt, params, rA, iA, rE, iE, stream=None):
+        """(grad, loss): the loss and parameter gradients of one batch of all
+        `count` matrices (device tensors; grad in checkpoint order)."""
+        import torch
+        grad = torch.empty(int(lib().ves_shiftnet_param_count(self.handle)), dtype=torch.float32, device=rA.device)
+        loss = torch.zeros(1, dtype=torch.float32, device=rA.device)
+        _check(lib().ves_shiftnet_gradient(self.handle, count, thread_cnt, _dp(params), _dp(rA), _dp(iA), _dp(rE),
+                                           _dp(iE), _dp(grad), _dp(loss), _stream_ptr(stream)),
+               "ves_shiftnet_gradient")
+        return grad, loss
+
     def predict_workspace(self, count):
         return DeviceBuffer(lib().ves_shiftnet_predict_workspace_size(self.handle, count))
 
@@ -512,6 +526,15 @@ def fp64_fma_rate(stream=None):
     v = ctypes.c_double(0.0)
     _check(lib().ves_fp64_fma_rate(ctypes.byref(v), _stream_ptr(stream)), "ves_fp64_fma_rate")
     return v.value
+
+
+def partition_blocks(block_cnt, parts, part):
+    """(first_block, n_blocks): the contiguous range of whole SoA blocks that
+    part `part` of `parts` owns when one batch is split over several GPUs."""
+    f, nb = _int(0), _int(0)
+    _check(lib().ves_partition_blocks(block_cnt, parts, part, ctypes.byref(f), ctypes.byref(nb)),
+           "ves_partition_blocks")
+    return f.value, nb.value
 
 
 def fp32_fma_rate(stream=None):
