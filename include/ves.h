@@ -384,6 +384,16 @@ int ves_eigensolve_noalloc(int dim, int block_cnt, int thread_cnt,
  * VES_ERR_ARG for block_cnt < 0, parts < 1 or part outside [0, parts). */
 int ves_partition_blocks(int block_cnt, int parts, int part, int *first_block, int *n_blocks);
 
+/* Index violations counted by the bounds-checked build of this library
+ * (libves_bc.so, compiled with -DVES_BOUNDS_CHECK): every matrix and vector
+ * element access of the numerical routines checks its indices, counts one
+ * that is out of range and reads or writes the first element instead, so a
+ * kernel never touches memory outside its operand.  *count = the number since
+ * the last reset (reset != 0 clears the counters after reading; synchronous).
+ * The normal build returns VES_ERR_UNSUPPORTED.  No counterpart in the
+ * reference. */
+int ves_bounds_violations(unsigned long long *count, int reset);
+
 /* Last error message of the calling thread ("" if none). */
 const char *ves_last_error(void);
 /* Free the library's cached device buffers. */

@@ -131,3 +131,12 @@ def test_python_interface_mirrors_reference_module():
     m = np.arange(2 * 9 * 4, dtype=float)
     np.testing.assert_array_equal(pi.extractMatrix(3, 4, m), m[::4][:9].reshape(3, 3).T)
     np.testing.assert_array_equal(pi.extractVector(3, 4, m), m[::4][:3])
+
+
+def test_bounds_query_needs_the_checked_build():
+    """ves_bounds_violations counts only in the bounds-checked build
+    (libves_bc.so); the normal library says so instead of returning 0."""
+    import ctypes
+    cnt = ctypes.c_ulonglong(7)
+    assert ves.lib().ves_bounds_violations(ctypes.byref(cnt), 0) == -4  # VES_ERR_UNSUPPORTED
+    assert cnt.value == 0

@@ -452,6 +452,28 @@ namespace ves {
 void set_error_message(const char *msg) { t_last_error = msg ? msg : ""; }
 }  // namespace ves
 
+#ifdef VES_BOUNDS_CHECK
+namespace {
+// the device counters of the bounds-checked build, one per translation unit
+struct BoundsRegistry {
+    std::mutex mu;
+    std::vector<std::pair<unsigned long long (*)(), void (*)()>> counters;
+};
+BoundsRegistry &bounds_registry()
+{
+    static BoundsRegistry r;  // constructed on first use: the units register during static initialisation
+    return r;
+}
+}  // namespace
+namespace ves {
+void register_bounds_counter(unsigned long long (*read)(), void (*reset)())
+{
+    std::lock_guard<std::mutex> lk(bounds_registry().mu);
+    bounds_registry().counters.emplace_back(read, reset);
+}
+}  // namespace ves
+#endif
+
 namespace ves {
 
 // The drop-in bodies behind the C names below and the C++ names of
@@ -1127,6 +1149,24 @@ int ves_fp32_fma_rate(double *flops_per_s, void *stream)
     begin_call();
     if (!flops_per_s) { set_error("null pointer"); return VES_ERR_ARG; }
     return native(cuda_ok(ves::fp32_fma_rate(flops_per_s, (cudaStream_t)stream), "fp32 probe"));
+}
+
+int ves_bounds_violations(unsigned long long *count, int reset)
+{
+    if (!count) { set_error("ves_bounds_violations: null pointer"); return VES_ERR_ARG; }
+    *count = 0;
+#ifdef VES_BOUNDS_CHECK
+    std::lock_guard<std::mutex> lk(bounds_registry().mu);
+    for (auto &c : bounds_registry().counters) {
+        *count += c.first();
+        if (reset) c.second();
+    }
+    return VES_OK;
+#else
+    (void)reset;
+    set_error("ves_bounds_violations: this library was built without VES_BOUNDS_CHECK");
+    return VES_ERR_UNSUPPORTED;
+#endif
 }
 
 int ves_partition_blocks(int block_cnt, int parts, int part, int *first_block, int *n_blocks)

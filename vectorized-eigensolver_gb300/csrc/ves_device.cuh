@@ -39,7 +39,22 @@ template <class R> __device__ __forceinline__ R cabs1(cx<R> z) { return fabs(z.r
 // helper, so the same expression could round differently in two kernels.
 // Written out, every kernel that inlines a helper computes the same bits
 // (the lane, warp-per-matrix and eigenvalues-only FP64 solvers rely on it).
-template <class R> __device__ __forceinline__ R cabs(cx<R> z) { return sqrt(fma(z.r, z.r, z.i * z.i)); }
+// Division, reciprocal and square root.  FP64: IEEE (the FP64 solvers give
+// the reference path's results, and the lane, warp-per-matrix and
+// eigenvalues-only kernels agree bit for bit).  FP32 (the Schur stage of the
+// FP32 + refinement form, the learned-shift polish): the hardware's fast
+// approximations (__fdividef: 2 ulp; x * rsqrtf(x): a few ulp) instead of the
+// IEEE sequences, which cost several times the instructions -- Newton's
+// method in FP64 corrects every FP32 eigenpair afterwards, so the FP32 stage
+// only has to give a good starting point.
+template <class R> __device__ __forceinline__ R fdiv(R a, R b) { return a / b; }
+template <> __device__ __forceinline__ float fdiv<float>(float a, float b) { return __fdividef(a, b); }
+template <class R> __device__ __forceinline__ R frcp(R x) { return R(1) / x; }
+template <> __device__ __forceinline__ float frcp<float>(float x) { return __fdividef(1.f, x); }
+template <class R> __device__ __forceinline__ R fsqrt(R x) { return sqrt(x); }
+template <> __device__ __forceinline__ float fsqrt<float>(float x) { return x > 0.f ? x * rsqrtf(x) : x; }
+
+template <class R> __device__ __forceinline__ R cabs(cx<R> z) { return fsqrt<R>(fma(z.r, z.r, z.i * z.i)); }
 template <class R> __device__ __forceinline__ cx<R> cmul(cx<R> a, cx<R> b) { return mk(fma(a.r, b.r, -(a.i * b.i)), fma(a.i, b.r, a.r * b.i)); }
 // a * conj(b)
 template <class R> __device__ __forceinline__ cx<R> cmulc(cx<R> a, cx<R> b) { return mk(fma(a.r, b.r, a.i * b.i), fma(a.i, b.r, -(a.r * b.i))); }
@@ -89,32 +104,32 @@ template <class R> __device__ __forceinline__ void rot_pair(cx<R> &h1, cx<R> &h2
 template <class R> __device__ __forceinline__ cx<R> cinv(cx<R> z)
 {
     if (fabs(z.r) <= fabs(z.i)) {
-        R ratio = z.r / z.i;
-        R rden = R(1) / (z.i * fma(ratio, ratio, R(1)));
+        R ratio = fdiv<R>(z.r, z.i);
+        R rden = frcp<R>(z.i * fma(ratio, ratio, R(1)));
         return mk(ratio * rden, -rden);
     } else {
-        R ratio = z.i / z.r;
-        R rden = R(1) / (z.r * fma(ratio, ratio, R(1)));
+        R ratio = fdiv<R>(z.i, z.r);
+        R rden = frcp<R>(z.r * fma(ratio, ratio, R(1)));
         return mk(rden, -ratio * rden);
     }
 }
 template <class R> __device__ __forceinline__ cx<R> cdiv(cx<R> a, cx<R> b)
 {
     if (fabs(b.r) <= fabs(b.i)) {
-        R ratio = b.r / b.i;
-        R rden = R(1) / (b.i * fma(ratio, ratio, R(1)));
+        R ratio = fdiv<R>(b.r, b.i);
+        R rden = frcp<R>(b.i * fma(ratio, ratio, R(1)));
         return mk(fma(a.r, ratio, a.i) * rden, fma(a.i, ratio, -a.r) * rden);
     } else {
-        R ratio = b.i / b.r;
-        R rden = R(1) / (b.r * fma(ratio, ratio, R(1)));
+        R ratio = fdiv<R>(b.i, b.r);
+        R rden = frcp<R>(b.r * fma(ratio, ratio, R(1)));
         return mk(fma(a.i, ratio, a.r) * rden, fma(-a.r, ratio, a.i) * rden);
     }
 }
 // principal square root (ComplexDouble.hpp:451-488 semantics)
 template <class R> __device__ __forceinline__ cx<R> csqrt(cx<R> z)
 {
-    R zr = sqrt(R(0.5) * (cabs(z) + fabs(z.r)));
-    R zi = (zr == R(0)) ? R(0) : fabs(z.i) / (R(2) * zr);
+    R zr = fsqrt<R>(R(0.5) * (cabs(z) + fabs(z.r)));
+    R zi = (zr == R(0)) ? R(0) : fdiv<R>(fabs(z.i), R(2) * zr);
     cx<R> w = (z.r < R(0)) ? mk(zi, zr) : mk(zr, zi);
     if (z.i < R(0)) w.i = -w.i;
     return w;
@@ -131,6 +146,50 @@ template <> struct lim<float> {
     static __device__ __forceinline__ float tiny() { return FLT_MIN; }
     static __device__ __forceinline__ float huge() { return FLT_MAX; }
 };
+
+// ---------------------------------------------------------------------------
+// Index checks of the bounds-checked build (-DVES_BOUNDS_CHECK; the library
+// variant libves_bc.so).  Every matrix accessor below checks 1 <= i, j <= n
+// and every vector accessor 1 <= i <= kMaxVecIndex; an index outside is
+// counted in this translation unit's device counter and the access goes to
+// the first element instead, so the kernel runs to its end and nothing is
+// read or written out of bounds.  ves_bounds_violations() sums the counters
+// of all translation units.  In the normal build the checks compile away.
+// ---------------------------------------------------------------------------
+#ifdef VES_BOUNDS_CHECK
+void register_bounds_counter(unsigned long long (*read)(), void (*reset)());
+namespace {
+__device__ unsigned long long g_bounds_violations;
+__device__ __noinline__ void bounds_hit() { atomicAdd(&g_bounds_violations, 1ULL); }
+struct BoundsCounterRegistration {
+    static unsigned long long read()
+    {
+        unsigned long long v = 0;
+        cudaMemcpyFromSymbol(&v, g_bounds_violations, sizeof v);
+        return v;
+    }
+    static void reset()
+    {
+        const unsigned long long z = 0;
+        cudaMemcpyToSymbol(g_bounds_violations, &z, sizeof z);
+    }
+    BoundsCounterRegistration() { register_bounds_counter(&read, &reset); }
+};
+const BoundsCounterRegistration g_bounds_registration;
+}  // namespace
+#define VES_CHECK_IJ(i, j, n)                                                   \
+    do {                                                                        \
+        if ((i) < 1 || (i) > (n) || (j) < 1 || (j) > (n)) { bounds_hit(); (i) = 1; (j) = 1; } \
+    } while (0)
+#define VES_CHECK_I(i)                                                          \
+    do {                                                                        \
+        if ((i) < 1 || (i) > kMaxVecIndex) { bounds_hit(); (i) = 1; }          \
+    } while (0)
+#else
+#define VES_CHECK_IJ(i, j, n) do { } while (0)
+#define VES_CHECK_I(i) do { } while (0)
+#endif
+constexpr int kMaxVecIndex = 128;  // vectors hold at most 2 n entries, n <= 64
 
 // ---------------------------------------------------------------------------
 // Matrix accessors.  Indices are 1-based (i = row, j = column), column-major.
@@ -152,15 +211,30 @@ template <class R> struct MatSoA {
     R *re, *im;
     long long s;
     int n;
-    __device__ __forceinline__ long long at(int i, int j) const { return ((long long)(i - 1) + (long long)(j - 1) * n) * s; }
+    __device__ __forceinline__ long long at(int i, int j) const
+    {
+        VES_CHECK_IJ(i, j, n);
+        return ((long long)(i - 1) + (long long)(j - 1) * n) * s;
+    }
     __device__ __forceinline__ cx<R> ld(int i, int j) const { long long k = at(i, j); return mk(re[k], im[k]); }
     __device__ __forceinline__ void st(int i, int j, cx<R> v) const { long long k = at(i, j); re[k] = v.r; im[k] = v.i; }
 };
 template <class R> struct VecSoA {
     R *re, *im;
     long long s;
-    __device__ __forceinline__ cx<R> ld(int i) const { long long k = (long long)(i - 1) * s; return mk(re[k], im[k]); }
-    __device__ __forceinline__ void st(int i, cx<R> v) const { long long k = (long long)(i - 1) * s; re[k] = v.r; im[k] = v.i; }
+    __device__ __forceinline__ cx<R> ld(int i) const
+    {
+        VES_CHECK_I(i);
+        long long k = (long long)(i - 1) * s;
+        return mk(re[k], im[k]);
+    }
+    __device__ __forceinline__ void st(int i, cx<R> v) const
+    {
+        VES_CHECK_I(i);
+        long long k = (long long)(i - 1) * s;
+        re[k] = v.r;
+        im[k] = v.i;
+    }
 };
 
 template <class R> struct vec2;
@@ -174,19 +248,31 @@ template <class R> struct MatIlv {
     int n;
     __device__ __forceinline__ cx<R> ld(int i, int j) const
     {
+        VES_CHECK_IJ(i, j, n);
         typename vec2<R>::T v = p[((i - 1) + (j - 1) * n) * 32];
         return mk(v.x, v.y);
     }
     __device__ __forceinline__ void st(int i, int j, cx<R> v) const
     {
+        VES_CHECK_IJ(i, j, n);
         typename vec2<R>::T w; w.x = v.r; w.y = v.i;
         p[((i - 1) + (j - 1) * n) * 32] = w;
     }
 };
 template <class R> struct VecIlv {
     typename vec2<R>::T *p;
-    __device__ __forceinline__ cx<R> ld(int i) const { typename vec2<R>::T v = p[(i - 1) * 32]; return mk(v.x, v.y); }
-    __device__ __forceinline__ void st(int i, cx<R> v) const { typename vec2<R>::T w; w.x = v.r; w.y = v.i; p[(i - 1) * 32] = w; }
+    __device__ __forceinline__ cx<R> ld(int i) const
+    {
+        VES_CHECK_I(i);
+        typename vec2<R>::T v = p[(i - 1) * 32];
+        return mk(v.x, v.y);
+    }
+    __device__ __forceinline__ void st(int i, cx<R> v) const
+    {
+        VES_CHECK_I(i);
+        typename vec2<R>::T w; w.x = v.r; w.y = v.i;
+        p[(i - 1) * 32] = w;
+    }
 };
 
 // ---------------------------------------------------------------------------
@@ -212,11 +298,11 @@ __device__ void zgehrd_lane(const int n, const M &A, const V &tau)
             xnorm2 = fma(x.i, x.i, fma(x.r, x.r, xnorm2));
         }
         const bool trivial = (xnorm2 == R(0)) && (alpha.i == R(0));
-        const R beta = trivial ? alpha.r : -copysign(sqrt(fma(alpha.r, alpha.r, fma(alpha.i, alpha.i, xnorm2))), alpha.r);
+        const R beta = trivial ? alpha.r : -copysign(fsqrt<R>(fma(alpha.r, alpha.r, fma(alpha.i, alpha.i, xnorm2))), alpha.r);
         cx<R> t = mk(R(0), R(0));
         cx<R> scale = mk(R(0), R(0));
         if (!trivial) {
-            const R rb = R(1) / beta;
+            const R rb = frcp<R>(beta);
             t = mk((beta - alpha.r) * rb, -alpha.i * rb);
             scale = cinv(mk(alpha.r - beta, alpha.i));
         }
@@ -322,8 +408,8 @@ __device__ void make_subdiag_real_lane(const int n, const MH &H, const MZ &Z)
     for (int i = 2; i <= n; ++i) {
         const cx<R> h = H.ld(i, i - 1);
         if (h.i != R(0)) {
-            cx<R> sc = cscal(h, R(1) / cabs1(h));
-            sc = cscal(conj(sc), R(1) / cabs(sc));
+            cx<R> sc = cscal(h, frcp<R>(cabs1(h)));
+            sc = cscal(conj(sc), frcp<R>(cabs(sc)));
             H.st(i, i - 1, mk(cabs(h), R(0)));
             for (int j = i; j <= n; ++j) H.st(i, j, cmul(H.ld(i, j), sc));
             const int re = (i + 1) < n ? (i + 1) : n;
@@ -424,11 +510,11 @@ __device__ __forceinline__ cx<R> qr_shift(const int I, const int L, const int it
         const cx<R> x = cscal(csub(H.ld(I - 1, I - 1), t), R(0.5));
         const R sx = cabs1(x);
         s = fmax(s, sx);
-        const R rs = R(1) / s;
+        const R rs = frcp<R>(s);
         const cx<R> xs = cscal(x, rs), us = cscal(u, rs);
         cx<R> y = cscal(csqrt(cadd(cmul(xs, xs), cmul(us, us))), s);
         if (sx > R(0)) {
-            const R rsx = R(1) / sx;
+            const R rsx = frcp<R>(sx);
             if (fma(x.r * rsx, y.r, (x.i * rsx) * y.i) < R(0)) y = mk(-y.r, -y.i);
         }
         t = csub(t, cmul(cdiv(u, cadd(x, y)), u));
@@ -447,7 +533,7 @@ __device__ __forceinline__ void zlarfg2(cx<R> &v0, cx<R> &v1, cx<R> &t1)
         return;
     }
     const R safmin = lim<R>::tiny() / (lim<R>::eps() * R(0.5));
-    R norm = sqrt(fma(v1.i, v1.i, fma(v1.r, v1.r, fma(v0.i, v0.i, v0.r * v0.r))));
+    R norm = fsqrt<R>(fma(v1.i, v1.i, fma(v1.r, v1.r, fma(v0.i, v0.i, v0.r * v0.r))));
     int knt = 0;
     if (norm < safmin) {
         const R rs = R(1) / safmin;
@@ -457,11 +543,11 @@ __device__ __forceinline__ void zlarfg2(cx<R> &v0, cx<R> &v1, cx<R> &t1)
             v0 = cscal(v0, rs);
             norm *= rs;
         } while (norm < safmin && knt < 40);
-        norm = sqrt(fma(v1.i, v1.i, fma(v1.r, v1.r, fma(v0.i, v0.i, v0.r * v0.r))));
+        norm = fsqrt<R>(fma(v1.i, v1.i, fma(v1.r, v1.r, fma(v0.i, v0.i, v0.r * v0.r))));
     }
     R beta = copysign(norm, v0.r);
     const cx<R> z = mk(v0.r + beta, v0.i);
-    t1 = cscal(z, R(1) / beta);
+    t1 = cscal(z, frcp<R>(beta));
     v1 = cmul(v1, cinv(z));
     for (int q = 0; q < knt; ++q) beta *= safmin;
     v0 = mk(-beta, R(0));
@@ -479,15 +565,29 @@ struct SmemMat {
     int lda;
     __device__ __forceinline__ cx<float> ld(int i, int j) const
     {
+        VES_CHECK_IJ(i, j, lda - 1);
         const float2 v = p[(i - 1) + (j - 1) * lda];
         return mk(v.x, v.y);
     }
-    __device__ __forceinline__ void st(int i, int j, cx<float> v) const { p[(i - 1) + (j - 1) * lda] = make_float2(v.r, v.i); }
+    __device__ __forceinline__ void st(int i, int j, cx<float> v) const
+    {
+        VES_CHECK_IJ(i, j, lda - 1);
+        p[(i - 1) + (j - 1) * lda] = make_float2(v.r, v.i);
+    }
 };
 struct SmemCol {  // column of a SmemMat as a vector
     float2 *p;
-    __device__ __forceinline__ cx<float> ld(int i) const { const float2 v = p[i - 1]; return mk(v.x, v.y); }
-    __device__ __forceinline__ void st(int i, cx<float> v) const { p[i - 1] = make_float2(v.r, v.i); }
+    __device__ __forceinline__ cx<float> ld(int i) const
+    {
+        VES_CHECK_I(i);
+        const float2 v = p[i - 1];
+        return mk(v.x, v.y);
+    }
+    __device__ __forceinline__ void st(int i, cx<float> v) const
+    {
+        VES_CHECK_I(i);
+        p[i - 1] = make_float2(v.r, v.i);
+    }
 };
 
 // Sum over a group of G lanes (G = 32: the warp; G = 16: one half of it);
@@ -521,10 +621,10 @@ __device__ __forceinline__ void hess_group(const int n, const SmemMat &H, float2
         const float xnorm2 = group_sum<G>(fmaf(xk.i, xk.i, xk.r * xk.r), mask);
         const cx<float> alpha = H.ld(i + 1, i);
         const bool trivial = (xnorm2 == 0.f) && (alpha.i == 0.f);
-        const float beta = trivial ? alpha.r : -copysignf(sqrtf(fmaf(alpha.r, alpha.r, fmaf(alpha.i, alpha.i, xnorm2))), alpha.r);
+        const float beta = trivial ? alpha.r : -copysignf(fsqrt<float>(fmaf(alpha.r, alpha.r, fmaf(alpha.i, alpha.i, xnorm2))), alpha.r);
         cx<float> t = mk(0.f, 0.f), scale = mk(0.f, 0.f);
         if (!trivial) {
-            const float rb = 1.f / beta;
+            const float rb = frcp<float>(beta);
             t = mk((beta - alpha.r) * rb, -alpha.i * rb);
             scale = cinv(mk(alpha.r - beta, alpha.i));
         }
@@ -725,7 +825,7 @@ __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool va
                 if (sp) sp->template pick<R>(its, I, t, fabs(H.ld(I, I - 1).r));
                 const cx<R> h11s = csub(H.ld(L, L), t);
                 const R h21 = H.ld(L + 1, L).r;
-                const R rs = R(1) / (cabs1(h11s) + fabs(h21));
+                const R rs = frcp<R>(cabs1(h11s) + fabs(h21));
                 v0 = cscal(h11s, rs);
                 v1 = mk(h21 * rs, R(0));
                 sweep = true;
@@ -812,7 +912,7 @@ __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool va
             const cx<R> h = H.ld(I, I - 1);
             if (h.i != R(0)) {
                 const R d = cabs(h);
-                const cx<R> z = conj(cscal(h, R(1) / d));
+                const cx<R> z = conj(cscal(h, frcp<R>(d)));
                 H.st(I, I - 1, mk(d, R(0)));
                 if (kSchur)
                     for (int j = I + 1; j <= n; ++j) H.st(I, j, cmul(H.ld(I, j), z));

@@ -196,15 +196,29 @@ struct SmemMat64 {
     int lda;
     __device__ __forceinline__ cx<double> ld(int i, int j) const
     {
+        VES_CHECK_IJ(i, j, lda - 1);
         const double2 v = p[(i - 1) + (j - 1) * lda];
         return mk(v.x, v.y);
     }
-    __device__ __forceinline__ void st(int i, int j, cx<double> v) const { p[(i - 1) + (j - 1) * lda] = make_double2(v.r, v.i); }
+    __device__ __forceinline__ void st(int i, int j, cx<double> v) const
+    {
+        VES_CHECK_IJ(i, j, lda - 1);
+        p[(i - 1) + (j - 1) * lda] = make_double2(v.r, v.i);
+    }
 };
 struct SmemCol64 {
     double2 *p;
-    __device__ __forceinline__ cx<double> ld(int i) const { const double2 v = p[i - 1]; return mk(v.x, v.y); }
-    __device__ __forceinline__ void st(int i, cx<double> v) const { p[i - 1] = make_double2(v.r, v.i); }
+    __device__ __forceinline__ cx<double> ld(int i) const
+    {
+        VES_CHECK_I(i);
+        const double2 v = p[i - 1];
+        return mk(v.x, v.y);
+    }
+    __device__ __forceinline__ void st(int i, cx<double> v) const
+    {
+        VES_CHECK_I(i);
+        p[i - 1] = make_double2(v.r, v.i);
+    }
 };
 
 // double2 elements of shared memory: H, Z, X (n (n + 1) each), tau, scales

@@ -300,8 +300,8 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
             for (int i = 2; i <= n; ++i) {
                 const cx<float> h = H.ld(i, i - 1);
                 if (h.i != 0.f) {
-                    cx<float> sc = cscal(h, 1.f / cabs1(h));
-                    sc = cscal(conj(sc), 1.f / cabs(sc));
+                    cx<float> sc = cscal(h, frcp<float>(cabs1(h)));
+                    sc = cscal(conj(sc), frcp<float>(cabs(sc)));
                     __syncwarp(gmask);
                     if (gl == 0) H.st(i, i - 1, mk(cabs(h), 0.f));
                     if (j >= i && j <= n) H.st(i, j, cmul(H.ld(i, j), sc));
@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
                 const cx<float> t = qr_shift<float>(I, L, its, H);
                 const cx<float> h11s = csub(H.ld(L, L), t);
                 const float h21 = H.ld(L + 1, L).r;
-                const float rs = 1.f / (cabs1(h11s) + fabsf(h21));
+                const float rs = frcp<float>(cabs1(h11s) + fabsf(h21));
                 const cx<float> v0 = cscal(h11s, rs), v1 = mk(h21 * rs, 0.f);
                 ++its;
                 ++sweeps;
@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
                 const cx<float> h = H.ld(I, I - 1);
                 if (h.i != 0.f) {
                     const float d = cabs(h);
-                    const cx<float> z = conj(cscal(h, 1.f / d));
+                    const cx<float> z = conj(cscal(h, frcp<float>(d)));
                     __syncwarp(gmask);
                     if (gl == 0) H.st(I, I - 1, mk(d, 0.f));
                     if (j >= I + 1 && j <= n) H.st(I, j, cmul(H.ld(I, j), z));
@@ -504,10 +504,10 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
             const float xnorm2 = group_sum<G>(xs, gmask);
             const cx<float> alpha = H.ld(i + 1, i);
             const bool trivial = (xnorm2 == 0.f) && (alpha.i == 0.f);
-            const float beta = trivial ? alpha.r : -copysignf(sqrtf(fmaf(alpha.r, alpha.r, fmaf(alpha.i, alpha.i, xnorm2))), alpha.r);
+            const float beta = trivial ? alpha.r : -copysignf(fsqrt<float>(fmaf(alpha.r, alpha.r, fmaf(alpha.i, alpha.i, xnorm2))), alpha.r);
             cx<float> t = mk(0.f, 0.f), scale = mk(0.f, 0.f);
             if (!trivial) {
-                const float rb = 1.f / beta;
+                const float rb = frcp<float>(beta);
                 t = mk((beta - alpha.r) * rb, -alpha.i * rb);
                 scale = cinv(mk(alpha.r - beta, alpha.i));
             }
@@ -570,8 +570,8 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
             const cx<float> h = H.ld(i, i - 1);
             __syncwarp(gmask);
             if (h.i != 0.f) {  // the same on every lane of the group
-                cx<float> sc = cscal(h, 1.f / cabs1(h));
-                sc = cscal(conj(sc), 1.f / cabs(sc));
+                cx<float> sc = cscal(h, frcp<float>(cabs1(h)));
+                sc = cscal(conj(sc), frcp<float>(cabs(sc)));
                 H.st(i, i - 1, mk(cabs(h), 0.f));
                 for (int j = j0; j <= n; j += G)
                     if (j >= i) H.st(i, j, cmul(H.ld(i, j), sc));
@@ -602,7 +602,7 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
                     const cx<float> t = qr_shift<float>(I, L, its, H);
                     const cx<float> h11s = csub(H.ld(L, L), t);
                     const float h21 = H.ld(L + 1, L).r;
-                    const float rs = 1.f / (cabs1(h11s) + fabsf(h21));
+                    const float rs = frcp<float>(cabs1(h11s) + fabsf(h21));
                     v0 = cscal(h11s, rs);
                     v1 = mk(h21 * rs, 0.f);
                     sweep = true;
@@ -657,7 +657,7 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
             __syncwarp();
             if (sweep && h.i != 0.f) {
                 const float d = cabs(h);
-                const cx<float> z = conj(cscal(h, 1.f / d));
+                const cx<float> z = conj(cscal(h, frcp<float>(d)));
                 H.st(I, I - 1, mk(d, 0.f));
                 for (int j = j0; j <= n; j += G) {
                     if (j >= I + 1) H.st(I, j, cmul(H.ld(I, j), z));
@@ -705,6 +705,7 @@ template <int S> struct MatBuf {
     int n;
     __device__ __forceinline__ cx<float> ld(int i, int j) const
     {
+        VES_CHECK_IJ(i, j, n);
         const float2 v = p[((i - 1) + (j - 1) * n) * S];
         return mk(v.x, v.y);
     }
@@ -961,7 +962,6 @@ int schur_group(int n)
     if (e && !strcmp(e, "warp32")) return n <= 32 ? 32 : 0;
     if (e && !strcmp(e, "group4")) return n <= 16 ? 4 : 0;
     if (e && !strcmp(e, "group8")) return n <= 16 ? 8 : 0;
-    if (n <= 16) return 8;
     return (n >= 24 && n <= 32) ? 32 : 0;
 }
 

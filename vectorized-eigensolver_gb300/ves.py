@@ -13,7 +13,9 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIBPATH = os.path.join(HERE, "libves.so")
+# VES_LIBRARY selects another build of the library (the bounds-checked
+# libves_bc.so that build.py makes with variant="bc")
+LIBPATH = os.environ.get("VES_LIBRARY") or os.path.join(HERE, "libves.so")
 
 VES_STATUS_ITCAP = 1
 VES_STATUS_NONFINITE = 2
@@ -110,6 +112,7 @@ SIGNATURES = {
     "ves_complex_from_soa_vec": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP]),
     "ves_eigensolve_noalloc": (_int, [_int, _int, _int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "ves_partition_blocks": (_int, [_int, _int, _int, ctypes.POINTER(_int), ctypes.POINTER(_int)]),
+    "ves_bounds_violations": (_int, [ctypes.POINTER(ctypes.c_ulonglong), _int]),
     "ves_last_error": (ctypes.c_char_p, []),
     "ves_release": (None, []),
     "ves_version": (_int, []),
