@@ -281,14 +281,15 @@ def test_mixed_work_counters():
     assert polish == 0
 
 
-def test_mixed_concurrent_callers():
+def test_mixed_concurrent_callers(monkeypatch):
     """Two host threads, each with its own stream and workspace, run the
-    FP32+refine form at once (large enough for the overlapped two-stream
-    path, whose library streams they share): each gets the result of a call
+    FP32+refine form at once on the overlapped two-stream path (forced on;
+    the threads share its library streams): each gets the result of a call
     made alone, bit for bit."""
     import threading
 
     import torch
+    monkeypatch.setenv("VES_MIXED_OVERLAP", "1")
     n, N, tc = 8, 65536, 512
     batches = [workloads.gaussian_soa(N, n, s, tc) for s in (41, 42)]
     opt = ves.default_options(precision=MIX)
@@ -319,11 +320,13 @@ def test_mixed_concurrent_callers():
             np.testing.assert_array_equal(a, b)
 
 
-def test_mixed_graph_capture():
+def test_mixed_graph_capture(monkeypatch):
     """A FP32+refine call captured in a CUDA graph (it stays on the capturing
-    stream instead of forking the shared library streams) replays to the
-    result of a direct call, bit for bit."""
+    stream instead of forking the shared library streams, which it would do
+    uncaptured: overlap forced on) replays to the result of a direct call, bit
+    for bit."""
     import torch
+    monkeypatch.setenv("VES_MIXED_OVERLAP", "1")
     n, N, tc = 8, 65536, 512
     rA, iA = workloads.gaussian_soa(N, n, 43, tc)
     dA = [torch.from_numpy(x).cuda() for x in (rA, iA)]

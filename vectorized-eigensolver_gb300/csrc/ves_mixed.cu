@@ -941,8 +941,15 @@ size_t mixed_workspace_bytes(int n, long long N, int blocks_per_sm, int *out_blo
 
 namespace {
 
-// Which FP32 Schur kernel: 0 = schur32_kernel (a matrix per lane), G = 16 or
-// 32 = schur32_warp_kernel<G> (a matrix per G lanes).  Measured on GB300,
+// Which FP32 Schur kernel: 0 = schur32_kernel (a matrix per lane), G = 4 or
+// 8 = schur32_group_kernel<G>, G = 16 or 32 = schur32_warp_kernel<G> (a
+// matrix per G lanes).  With the fast FP32 division and square root, measured
+// on GB300 (FP32+refine eigensolves/s, stages in sequence, two float-float
+// steps): n=8 lane 47.9, group4 43.0, group8 36.1 M/s; n=12 lane 14.4,
+// group4 15.4, group8 12.9 M/s; n=16 lane 6.10 (6.43 overlapped), group4
+// 6.78, group8 7.04 M/s.  Default: the group kernel with G = 4 for
+// 11 <= n <= 13 and G = 8 for 14 <= n <= 16.  Older measurements, before the
+// fast FP32 arithmetic and the group kernels:  Measured on GB300,
 // FP32+refine eigensolves/s, lane -> warp (G = 32): n=16 5.34 -> 4.26 M/s,
 // n=24 1.59 -> 1.63 M/s, n=32 0.66 -> 0.72 M/s (below 24 too many lanes of a
 // warp idle).  Two matrices per warp (G = 16) does not recover it: with the
@@ -962,6 +969,8 @@ int schur_group(int n)
     if (e && !strcmp(e, "warp32")) return n <= 32 ? 32 : 0;
     if (e && !strcmp(e, "group4")) return n <= 16 ? 4 : 0;
     if (e && !strcmp(e, "group8")) return n <= 16 ? 8 : 0;
+    if (n >= 11 && n <= 13) return 4;
+    if (n >= 14 && n <= 16) return 8;
     return (n >= 24 && n <= 32) ? 32 : 0;
 }
 
