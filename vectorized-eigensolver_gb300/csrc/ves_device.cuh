@@ -454,7 +454,9 @@ __device__ __forceinline__ int deflation_scan(const int I, const int L0, const M
 // them: its sums and products round by a few 2^-24 relative, far inside the
 // 2^-20 margin, so the FP64 evaluation would decide the same.  Only the
 // others (the subdiagonals at or near deflation, and tst = 0) are tested in
-// FP64, so the decisions are those of a full FP64 evaluation.
+// FP64, so the decisions are those of a full FP64 evaluation.  The
+// Ahues-Tisseur comparison is the reference's multiplied through by its
+// positive denominator (the same test, without divisions).
 template <class MH>
 __device__ __forceinline__ int deflation_scan64(const int I, const int L0, const MH &H, const int n, const float ulp,
                                                 const float smlnum)
@@ -475,6 +477,9 @@ __device__ __forceinline__ int deflation_scan64(const int I, const int L0, const
             if (K + 1 <= n) tst += fabs((double)H.ld(K + 1, K).r);
         }
         if (fabs(hk.r) <= ulp64 * tst) {
+            // Ahues-Tisseur: ba (ab / s) <= max(smlnum, ulp bb (aa / s)), s = aa + ab > 0,
+            // multiplied through by s: no division (two FP64 division sequences a
+            // test), and on FP32 data the sums and products are exact in FP64
             const cx<float> hkuf = H.ld(K - 1, K);
             double d2 = cabs1(hk), d3 = cabs1(mk((double)hkuf.r, (double)hkuf.i));
             const double ab = fmax(d2, d3), ba = fmin(d2, d3);
@@ -482,7 +487,7 @@ __device__ __forceinline__ int deflation_scan64(const int I, const int L0, const
             d3 = cabs1(csub(hkm, hkk));
             const double aa = fmax(d2, d3), bb = fmin(d2, d3);
             const double s = aa + ab;
-            if (ba * (ab / s) <= fmax(sml64, ulp64 * (bb * (aa / s)))) break;
+            if (ba * ab <= fmax(sml64 * s, ulp64 * (bb * aa))) break;
         }
     }
     return K;
@@ -525,6 +530,24 @@ __device__ __forceinline__ cx<R> qr_shift(const int I, const int L, const int it
 // 2-element Householder reflector for (v0, v1) (reference :186-241, LAPACK
 // zlarfg with n = 2).  Returns tau in t1, overwrites v1 with the scaled vector
 // entry and v0 with the new leading entry.
+//
+// It runs once per bulge-chase step, so its divisions and square root cost
+// a noticeable share of the FP64 pipe (each is a sequence of several FP64
+// instructions).  When |(v0, v1)|^2 is a comfortably normal number -- every
+// case but the tiny or huge vectors that need the reference's rescaling --
+// one reciprocal square root gives both beta = +-norm and 1/beta, and
+// 1/z (z = v0 + beta) comes from tau = z/beta, whose real part lies in
+// [1, 2]: 1/z = conj(tau) (1/beta) / |tau|^2, one more reciprocal.  Two
+// reciprocal sequences replace the reference's square root, reciprocal and
+// Smith division (a division and a reciprocal); the reflector is the same up
+// to rounding.
+template <class R> __device__ __forceinline__ R frsqrt(R x);
+template <> __device__ __forceinline__ double frsqrt<double>(double x) { return rsqrt(x); }
+template <> __device__ __forceinline__ float frsqrt<float>(float x) { return rsqrtf(x); }
+template <class R> struct rfl_range;  // |(v0, v1)|^2 range of the fast path
+template <> struct rfl_range<double> { static __device__ __forceinline__ double lo() { return 1e-290; } };
+template <> struct rfl_range<float> { static __device__ __forceinline__ float lo() { return 1e-36f; } };
+
 template <class R>
 __device__ __forceinline__ void zlarfg2(cx<R> &v0, cx<R> &v1, cx<R> &t1)
 {
@@ -532,8 +555,18 @@ __device__ __forceinline__ void zlarfg2(cx<R> &v0, cx<R> &v1, cx<R> &t1)
         t1 = mk(R(0), R(0));
         return;
     }
+    const R nrm2 = fma(v1.i, v1.i, fma(v1.r, v1.r, fma(v0.i, v0.i, v0.r * v0.r)));
+    if (nrm2 >= rfl_range<R>::lo() && nrm2 <= lim<R>::huge()) {
+        const R rn = frsqrt<R>(nrm2);  // 1 / norm
+        const R beta = copysign(nrm2 * rn, v0.r), rb = copysign(rn, v0.r);
+        t1 = cscal(mk(v0.r + beta, v0.i), rb);  // tau = z / beta
+        const R q = rb * frcp<R>(fma(t1.r, t1.r, t1.i * t1.i));
+        v1 = cmul(v1, mk(t1.r * q, -t1.i * q));  // v1 / z
+        v0 = mk(-beta, R(0));
+        return;
+    }
     const R safmin = lim<R>::tiny() / (lim<R>::eps() * R(0.5));
-    R norm = fsqrt<R>(fma(v1.i, v1.i, fma(v1.r, v1.r, fma(v0.i, v0.i, v0.r * v0.r))));
+    R norm = fsqrt<R>(nrm2);
     int knt = 0;
     if (norm < safmin) {
         const R rs = R(1) / safmin;

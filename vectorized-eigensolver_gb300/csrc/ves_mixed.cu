@@ -425,8 +425,11 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
 // warp-uniform over the union of the groups' windows, and a group whose
 // window does not contain K idles for that step.  Values that all lanes of a
 // group write to one location (a zeroed subdiagonal, a reflector's leading
-// entry) are computed identically on every lane, so no lane can read a stale
-// copy.
+// entry) are stored by the group's first lane before a synchronisation point
+// (one lane per address: several lanes storing to one shared-memory word cost
+// extra wavefronts), except the zeroed subdiagonal of the deflation scan,
+// which every lane of the group stores with the same value (no
+// synchronisation inside the per-group scan).
 //
 // Same algorithm per element as the lane routines (zgehd2, zung2r, zlahqr
 // single shift with the FP64 deflation test, ztrevc back substitution), in a
@@ -514,7 +517,7 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
             __syncwarp(gmask);  // every lane has read column i
             for (int k = j0; k <= n; k += G)
                 if (k >= i + 2) H.st(k, i, cmul(H.ld(k, i), scale));
-            sTau[i - 1] = make_float2(t.r, t.i);
+            if (gl == 0) sTau[i - 1] = make_float2(t.r, t.i);
             __syncwarp(gmask);
             for (int r = j0; r <= n; r += G) {  // right: row r of A(1:n, i+1:n) -= tau (A v)_r v^H
                 cx<float> sacc = H.ld(r, i + 1);
@@ -534,7 +537,7 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
                 for (int q = 2; q <= mm; ++q) H.st(i + q, c, cnmac(H.ld(i + q, c), H.ld(i + q, i), ts));
             }
             __syncwarp(gmask);
-            H.st(i + 1, i, mk(beta, 0.f));
+            if (gl == 0) H.st(i + 1, i, mk(beta, 0.f));
             __syncwarp(gmask);
         }
         // ---- zung2r: Z = Q from the reflectors, last reflector first
@@ -572,7 +575,7 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
             if (h.i != 0.f) {  // the same on every lane of the group
                 cx<float> sc = cscal(h, frcp<float>(cabs1(h)));
                 sc = cscal(conj(sc), frcp<float>(cabs(sc)));
-                H.st(i, i - 1, mk(cabs(h), 0.f));
+                if (gl == 0) H.st(i, i - 1, mk(cabs(h), 0.f));
                 for (int j = j0; j <= n; j += G)
                     if (j >= i) H.st(i, j, cmul(H.ld(i, j), sc));
                 __syncwarp(gmask);
@@ -623,7 +626,7 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
                     zlarfg2<float>(a0, a1, t1);
                 }
                 __syncwarp();  // every lane has read H(K, K-1), H(K+1, K-1)
-                if (act && K > L) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(0.f, 0.f)); }
+                if (act && K > L && gl == 0) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(0.f, 0.f)); }
                 const cx<float> w1 = a1, cw = conj(w1), c1 = conj(t1);
                 const float t2 = fmaf(t1.r, w1.r, -(t1.i * w1.i));
                 if (act) {
@@ -658,7 +661,7 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
             if (sweep && h.i != 0.f) {
                 const float d = cabs(h);
                 const cx<float> z = conj(cscal(h, frcp<float>(d)));
-                H.st(I, I - 1, mk(d, 0.f));
+                if (gl == 0) H.st(I, I - 1, mk(d, 0.f));
                 for (int j = j0; j <= n; j += G) {
                     if (j >= I + 1) H.st(I, j, cmul(H.ld(I, j), z));
                     if (j <= I - 1) H.st(j, I, cmulc(H.ld(j, I), z));
