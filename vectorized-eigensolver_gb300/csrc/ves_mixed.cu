@@ -718,11 +718,10 @@ template <int S> struct MatBuf {
 // memory, indexed uniformly across the warp).  kPerMatrix: the Schur buffer
 // has the per-matrix layout.
 template <int MAXN, bool kPerMatrix>
-__global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs a, const float2 *buf, int *flags)
+__device__ __forceinline__ void refine_tile(const MixedArgs &a, const float2 *buf, int *flags, const long long tile)
 {
     const int n = a.g.n, tc = a.g.tc;
-    const long long N = a.g.N;
-    const long long p = a.m_begin * n + (long long)blockIdx.x * kRefineThreads + threadIdx.x;
+    const long long p = a.m_begin * n + tile * kRefineThreads + threadIdx.x;
     const bool valid = p < a.m_end * n;
     const long long m = valid ? p / n : 0;
     const int k = valid ? (int)(p % n) + 1 : 1;
@@ -864,6 +863,18 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
     }
     const MatSoA<double> Vo{a.rV + mo, a.iV + mo, tc, n};
     for (int i = 1; i <= n; ++i) Vo.st(i, k, cscal(v[i - 1], scale));
+}
+
+// Tiles of kRefineThreads pairs, block-strided: the grid is either one block
+// per tile or a persistent grid whose size bounds the resident warps (the
+// per-pair vectors live in local memory; fewer resident threads keep more of
+// them in L1).
+template <int MAXN, bool kPerMatrix>
+__global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs a, const float2 *buf, int *flags)
+{
+    const long long ntiles = ((a.m_end - a.m_begin) * a.g.n + kRefineThreads - 1) / kRefineThreads;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+        refine_tile<MAXN, kPerMatrix>(a, buf, flags, tile);
 }
 
 // Distinctness of the refined eigenvalues of each matrix.  Newton from two
@@ -1060,7 +1071,13 @@ cudaError_t launch_refine(const MixedArgs &a, cudaStream_t st)
     const int n = a.g.n;
     const MixedBufs b = mixed_bufs(a);
     const long long pairs = (a.m_end - a.m_begin) * n;
-    const unsigned rb = (unsigned)((pairs + kRefineThreads - 1) / kRefineThreads);
+    long long tiles = (pairs + kRefineThreads - 1) / kRefineThreads;
+    // VES_REFINE_BLOCKS_PER_SM (tuning): a persistent grid of that many blocks per SM
+    if (const char *e = getenv("VES_REFINE_BLOCKS_PER_SM")) {
+        const int v = atoi(e);
+        if (v >= 1 && v <= 32) tiles = std::min<long long>(tiles, (long long)device_sms() * v);
+    }
+    const unsigned rb = (unsigned)std::max<long long>(1, tiles);
     if (schur_group(n)) {  // per-matrix buffer layout
         if (n <= 16)
             refine_kernel<16, true><<<rb, kRefineThreads, 0, st>>>(a, b.buf, b.flags);
