@@ -74,6 +74,10 @@ cudaError_t launch_gemm_bf16(int M, int N, int K, const void *A, int lda, const 
     auto *c = static_cast<__nv_bfloat16 *>(C);
     const bool vec_ok = (N % 16) == 0 && (ldc % 8) == 0 && ((uintptr_t)C & 15) == 0 && ((uintptr_t)Cf & 15) == 0;
     if (K % 16 == 0 && K <= 256 && vec_ok) {
+        // few row tiles (a training batch): narrower column tiles give more CTAs
+        // (M = 1,024, N = 256: 32 instead of 8)
+        if ((M + tc::kM - 1) / tc::kM <= 16 && N > 64 && N % 64 == 0)
+            return launch_persistent<64>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
         if (N > 128) return launch_persistent<256>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
         if (N > 64) return launch_persistent<128>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
         return launch_persistent<64>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
@@ -121,96 +125,91 @@ __device__ __forceinline__ long long soa_off_s(long long m, long long len, int t
 }
 
 constexpr int kMaxFourier = 64;  // n_params * fourier
-constexpr int kMaxFeat = 64 + 2 * kMaxFourier + 3 * kMaxDimNet;
 
-// raw (unnormalised) features of matrix m into f[0 .. P + 2PF + 2n + S(n-1)):
-// parameters, sin / cos ((pi/2) k p) for k = 1..F, Re diag A, Im diag A, and
+// feature c (unnormalised) of matrix m; the row is [parameters (P), sin / cos
+// ((pi/2) k p) for k = 1..F per parameter, Re diag A (n), Im diag A (n), and
 // with S = 1 the 2-norms of the n - 1 subdiagonals of A (how far A is from
-// upper triangular, diagonal by diagonal)
-__device__ __forceinline__ void raw_features(long long m, int n, int P, int F, int S, int tc, const double *params,
-                                             const double *rA, const double *iA, float *f)
+// upper triangular, diagonal by diagonal)]
+__device__ __forceinline__ float one_feature(long long m, int c, int n, int P, int F, int tc, const double *params,
+                                             const double *rA, const double *iA)
 {
-    for (int q = 0; q < P; ++q) {
-        const float x = params ? (float)params[m * P + q] : 0.f;
-        f[q] = x;
-        for (int k = 1; k <= F; ++k) {
-            float sn, cs;
-            sincospif(0.5f * (float)k * x, &sn, &cs);
-            f[P + 2 * (q * F + k - 1)] = sn;
-            f[P + 2 * (q * F + k - 1) + 1] = cs;
-        }
-    }
+    if (c < P) return params ? (float)params[m * P + c] : 0.f;
     const int o = P + 2 * P * F;
+    if (c < o) {
+        const int idx = c - P, q = idx / (2 * F), k = (idx % (2 * F)) / 2 + 1;
+        const float x = params ? (float)params[m * P + q] : 0.f;
+        float sn, cs;
+        sincospif(0.5f * (float)k * x, &sn, &cs);
+        return (idx & 1) ? cs : sn;
+    }
     const long long mo = soa_off_s(m, (long long)n * n, tc);
-    for (int i = 0; i < n; ++i) {
+    if (c < o + 2 * n) {
+        const int i = (c - o) % n;
         const long long k = mo + (long long)(i + i * n) * tc;
-        f[o + i] = (float)rA[k];
-        f[o + n + i] = (float)iA[k];
+        return c < o + n ? (float)rA[k] : (float)iA[k];
     }
-    if (S) {
-        for (int d = 1; d < n; ++d) {  // subdiagonal d: elements (i + d, i)
-            double s2 = 0.0;
-            for (int i = 0; i + d < n; ++i) {
-                const long long k = mo + (long long)(i + d + i * n) * tc;
-                s2 = fma(rA[k], rA[k], fma(iA[k], iA[k], s2));
-            }
-            f[o + 2 * n + d - 1] = (float)sqrt(s2);
-        }
+    const int d = c - o - 2 * n + 1;  // subdiagonal d: elements (i + d, i)
+    double s2 = 0.0;
+    for (int i = 0; i + d < n; ++i) {
+        const long long k = mo + (long long)(i + d + i * n) * tc;
+        s2 = fma(rA[k], rA[k], fma(iA[k], iA[k], s2));
     }
+    return (float)sqrt(s2);
 }
 
-// features -> standardised BF16 rows [count x kin_pad]
+// features -> standardised BF16 rows [count x kin_pad]: one warp per row, the
+// lanes take the row's features c = lane, lane + 32, ... (coalesced stores)
 __global__ void features_kernel(long long count, int n, int P, int F, int S, int tc, const double *params, const double *rA,
                                 const double *iA, const float *mean, const float *stdv, int kin, int kin_pad, bf16 *X,
                                 const int *rows)
 {
-    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (r >= count) return;
     const long long m = rows ? rows[r] : r;
-    float f[kMaxFeat];
-    raw_features(m, n, P, F, S, tc, params, rA, iA, f);
-    for (int c = 0; c < kin_pad; ++c) {
+    for (int c = lane; c < kin_pad; c += 32) {
         float v = 0.f;
-        if (c < kin) v = mean ? (f[c] - mean[c]) / stdv[c] : f[c];
+        if (c < kin) {
+            const float f = one_feature(m, c, n, P, F, tc, params, rA, iA);
+            v = mean ? (f - mean[c]) / stdv[c] : f;
+        }
         X[r * kin_pad + c] = __float2bfloat16(v);
     }
 }
 
-// canonical target of matrix m: eigenvalues sorted by real part -> t[0..2n)
-__device__ __forceinline__ void raw_target(long long m, int n, int tc, const double *rE, const double *iE, float *t)
-{
-    const long long vo = soa_off_s(m, n, tc);
-    float re[kMaxDimNet], im[kMaxDimNet];
-    for (int i = 0; i < n; ++i) {
-        re[i] = (float)rE[vo + (long long)i * tc];
-        im[i] = (float)iE[vo + (long long)i * tc];
-    }
-    for (int i = 1; i < n; ++i) {  // insertion sort by real part
-        const float a = re[i], b = im[i];
-        int j = i - 1;
-        while (j >= 0 && re[j] > a) {
-            re[j + 1] = re[j];
-            im[j + 1] = im[j];
-            --j;
-        }
-        re[j + 1] = a;
-        im[j + 1] = b;
-    }
-    for (int i = 0; i < n; ++i) {
-        t[i] = re[i];
-        t[n + i] = im[i];
-    }
-}
-
+// standardised targets [count x nout_pad]: the eigenvalues in canonical order
+// (real parts ascending, ties in index order), real parts then imaginary
+// parts.  One warp per row; lane i holds eigenvalues i and i + 32 and finds
+// each one's place in that order by counting
 __global__ void targets_kernel(long long count, int n, int tc, const double *rE, const double *iE, const float *mean,
                                const float *stdv, int nout_pad, float *T, const int *rows)
 {
-    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (r >= count) return;
     const long long m = rows ? rows[r] : r;
-    float t[2 * kMaxDimNet];
-    raw_target(m, n, tc, rE, iE, t);
-    for (int c = 0; c < nout_pad; ++c) T[r * nout_pad + c] = c < 2 * n ? (mean ? (t[c] - mean[c]) / stdv[c] : t[c]) : 0.f;
+    const long long vo = soa_off_s(m, n, tc);
+    float re[2], im[2];
+    int rank[2] = {0, 0};
+    for (int h = 0; h < 2; ++h) {
+        const int i = lane + 32 * h;
+        re[h] = i < n ? (float)rE[vo + (long long)i * tc] : 0.f;
+        im[h] = i < n ? (float)iE[vo + (long long)i * tc] : 0.f;
+    }
+    for (int j = 0; j < n; ++j) {
+        const float v0 = __shfl_sync(FULL, re[0], j & 31), v1 = __shfl_sync(FULL, re[1], j & 31);
+        const float rj = j < 32 ? v0 : v1;
+        for (int h = 0; h < 2; ++h) rank[h] += (rj < re[h]) || (rj == re[h] && j < lane + 32 * h);
+    }
+    float *t = T + r * nout_pad;
+    for (int h = 0; h < 2; ++h) {
+        const int i = lane + 32 * h;
+        if (i >= n) continue;
+        const int c = rank[h];
+        t[c] = mean ? (re[h] - mean[c]) / stdv[c] : re[h];
+        t[n + c] = mean ? (im[h] - mean[n + c]) / stdv[n + c] : im[h];
+    }
+    for (int c = 2 * n + lane; c < nout_pad; c += 32) t[c] = 0.f;
 }
 
 // column mean and standard deviation of the BF16 feature table, one thread per column
@@ -353,22 +352,6 @@ __global__ void gelu_bwd_kernel(long long total, const float *dH, const float *Z
 __device__ __forceinline__ float to_f32(bf16 x) { return __bfloat162float(x); }
 __device__ __forceinline__ float to_f32(float x) { return x; }
 
-// dW[o][i] = sum_b dZ[b][o] * H[b][i];  db[o] = sum_b dZ[b][o] (column i == 0 thread)
-template <class HT>
-__global__ void dw_kernel(int B, int out, int in, const float *dZ, const HT *H, int ldh, float *dW, float *db)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, o = blockIdx.y;
-    if (o >= out) return;
-    float acc = 0.f, accb = 0.f;
-    for (int b = 0; b < B; ++b) {
-        const float g = dZ[(long long)b * out + o];
-        if (i < in) acc = fmaf(g, to_f32(H[(long long)b * ldh + i]), acc);
-        accb += g;
-    }
-    if (i < in) dW[(long long)o * in + i] = acc;
-    if (i == 0) db[o] = accb;
-}
-
 // FP32 activations of the last hidden layer: Hf = GELU(Z)
 __global__ void gelu_f32_kernel(long long total, const float *Z, float *Hf)
 {
@@ -378,28 +361,35 @@ __global__ void gelu_f32_kernel(long long total, const float *Z, float *Hf)
 
 // Output layer in FP32 on CUDA cores (no BF16 rounding of the last hidden
 // activations or of the output weights): Y[r][o] = b[o] + sum_i W[o][i]
-// GELU(Z[r][i]).  A block of 128 threads takes 32 rows: the rows' activations
-// are staged in shared memory (coalesced reads, GELU applied once), then lane
-// l of warp w computes row l for outputs w, w + 4, ... (the W row is a
-// broadcast read).
-constexpr int kOutRows = 32;
-__global__ void __launch_bounds__(128) dense_out_kernel(int rows, int out, int in, const float *Z, const float *W,
+// GELU(Z[r][i]).  A block of (32, 8) threads takes a 32-row x 32-output tile:
+// GELU(Z) and W are staged through shared memory 32 columns of the sum at a
+// time, each thread accumulates four outputs, starting from the bias and
+// adding the terms in index order.
+__global__ void __launch_bounds__(256) dense_out_kernel(int rows, int out, int in, const float *Z, const float *W,
                                                         const float *b, float *Y)
 {
-    extern __shared__ float hs[];  // [kOutRows][in + 1]
-    const int r0 = blockIdx.x * kOutRows, ld = in + 1;
-    for (int e = threadIdx.x; e < kOutRows * in; e += blockDim.x) {
-        const int r = e / in, i = e % in;
-        hs[r * ld + i] = r0 + r < rows ? tc::gelu(Z[(long long)(r0 + r) * in + i]) : 0.f;
+    __shared__ float As[32][33], Ws[32][33];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int r0 = blockIdx.y * 32, o0 = blockIdx.x * 32;
+    float acc[4];
+    for (int q = 0; q < 4; ++q) acc[q] = o0 + tx < out ? b[o0 + tx] : 0.f;
+    for (int k0 = 0; k0 < in; k0 += 32) {
+        for (int q = 0; q < 4; ++q) {
+            const int rr = ty + 8 * q, k = k0 + tx;
+            As[rr][tx] = (r0 + rr < rows && k < in) ? tc::gelu(Z[(long long)(r0 + rr) * in + k]) : 0.f;
+            Ws[rr][tx] = (o0 + rr < out && k < in) ? W[(long long)(o0 + rr) * in + k] : 0.f;
+        }
+        __syncthreads();
+        const int kmax = min(32, in - k0);
+        for (int kk = 0; kk < kmax; ++kk) {
+            const float w = Ws[tx][kk];
+            for (int q = 0; q < 4; ++q) acc[q] = fmaf(w, As[ty + 8 * q][kk], acc[q]);
+        }
+        __syncthreads();
     }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int r = r0 + lane;
-    for (int o = warp; o < out; o += 4) {
-        const float *w = W + (long long)o * in;
-        float acc = b[o];
-        for (int i = 0; i < in; ++i) acc = fmaf(w[i], hs[lane * ld + i], acc);
-        if (r < rows) Y[(long long)r * out + o] = acc;
+    for (int q = 0; q < 4; ++q) {
+        const int r = r0 + ty + 8 * q, o = o0 + tx;
+        if (r < rows && o < out) Y[(long long)r * out + o] = acc[q];
     }
 }
 
@@ -443,14 +433,56 @@ __global__ void sum_splits_kernel(long long n, int S, long long zs, const float 
     out[e] = acc;
 }
 
-// db[o] = sum_b dZ[b][o]
-__global__ void colsum_kernel(int B, int out, const float *dZ, float *db)
+// db[o] = sum_b dZ[b][o]: a block of 32 x 32 threads takes 32 columns, thread
+// (x, y) sums rows y, y + 32, ... of column x (coalesced), then the 32 partial
+// sums of a column are added in shared memory
+__global__ void __launch_bounds__(1024) colsum_kernel(int B, int out, const float *dZ, float *db)
 {
-    const int o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= out) return;
+    __shared__ float part[32][33];
+    const int o = blockIdx.x * 32 + threadIdx.x;
     float acc = 0.f;
-    for (int b = 0; b < B; ++b) acc += dZ[(long long)b * out + o];
-    db[o] = acc;
+    if (o < out)
+        for (int b = threadIdx.y; b < B; b += 32) acc += dZ[(long long)b * out + o];
+    part[threadIdx.y][threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.y == 0 && o < out) {
+        float s = 0.f;
+        for (int y = 0; y < 32; ++y) s += part[y][threadIdx.x];
+        db[o] = s;
+    }
+}
+
+// The FP32 output layer's weight gradient, part[z][o][i] = sum over the z-th
+// range of the batch of dY[b][o] Hf[b][i] (dY: B x M, Hf: B x N, row-major):
+// 32 x 32 output tiles staged through shared memory, the batch split over the
+// grid's z dimension; the caller sums the partials.  Block (32, 8), four
+// outputs per thread.
+__global__ void __launch_bounds__(256) sgemm_tn_splitk_kernel(int M, int N, int K, const float *A, int lda,
+                                                              const float *Bm, int ldb, float *part, int kz)
+{
+    __shared__ float As[32][33], Bs[32][33];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int m0 = blockIdx.y * 32, n0 = blockIdx.x * 32;
+    const int kb = blockIdx.z * kz, ke = min(K, kb + kz);
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int k0 = kb; k0 < ke; k0 += 32) {
+        for (int q = 0; q < 4; ++q) {
+            const int kk = ty + 8 * q, k = k0 + kk;
+            As[kk][tx] = (k < ke && m0 + tx < M) ? A[(long long)k * lda + m0 + tx] : 0.f;
+            Bs[kk][tx] = (k < ke && n0 + tx < N) ? Bm[(long long)k * ldb + n0 + tx] : 0.f;
+        }
+        __syncthreads();
+        for (int kk = 0; kk < 32; ++kk) {
+            const float bv = Bs[kk][tx];
+            for (int q = 0; q < 4; ++q) acc[q] = fmaf(As[kk][ty + 8 * q], bv, acc[q]);
+        }
+        __syncthreads();
+    }
+    float *p = part + (long long)blockIdx.z * M * N;
+    for (int q = 0; q < 4; ++q) {
+        const int mm = m0 + ty + 8 * q, nn = n0 + tx;
+        if (mm < M && nn < N) p[(long long)mm * N + nn] = acc[q];
+    }
 }
 
 __global__ void adam_kernel(long long n, float *p, const float *g, float *m, float *v, float lr, float b1, float b2,
@@ -505,7 +537,7 @@ void load_shiftnet_kernels()
     load_kernel(target_stats_kernel);
     load_kernel(chamfer_kernel);
     load_kernel(gelu_bwd_kernel);
-    load_kernel(dw_kernel<float>);
+    load_kernel(sgemm_tn_splitk_kernel);
     load_kernel(transpose_bf16_kernel<float>);
     load_kernel(transpose_bf16_kernel<bf16>);
     load_kernel(sum_splits_kernel);
@@ -642,8 +674,7 @@ cudaError_t forward(const ves_shiftnet *t, int rows, const ves::bf16 *X, const A
         const long long nh = (long long)rows * t->H;
         ves::gelu_f32_kernel<<<ves::nb(nh), 256, 0, st>>>(nh, a.Z[t->L - 1], a.Hf);
     }
-    const size_t smem = (size_t)ves::kOutRows * (t->H + 1) * sizeof(float);
-    ves::dense_out_kernel<<<ves::nb(rows, ves::kOutRows), 128, smem, st>>>(rows, t->nout_pad, t->H, a.Z[t->L - 1],
+    ves::dense_out_kernel<<<dim3(ves::nb(t->nout_pad, 32), ves::nb(rows, 32)), dim3(32, 8), 0, st>>>(rows, t->nout_pad, t->H, a.Z[t->L - 1],
                                                                          t->W[t->L], t->b[t->L], a.Y);
     return cudaGetLastError();
 }
@@ -695,7 +726,7 @@ struct GradBufs {
     ves::bf16 *dZt = nullptr;             // dZ transposed [H x batch]: A operand of dW = dZ^T Hin
     ves::bf16 *HinT = nullptr;            // the layer input transposed [max(kin_pad, H) x batch]
     ves::bf16 *WbT = nullptr;             // BF16 weights transposed [H x H]: B operand of dH
-    float *part = nullptr;                // split-K partials [splits x H x max(kin_pad, H)]
+    float *part = nullptr;                // split-K partials [splits x max(H, nout_pad) x max(kin_pad, H)]
     int splits = 1;
 };
 
@@ -712,7 +743,7 @@ bool grad_alloc(const ves_shiftnet *t, int batch, GradBufs &g)
               cudaMalloc(&g.dZt, (size_t)batch * H * 2) == cudaSuccess &&
               cudaMalloc(&g.HinT, (size_t)batch * imax * 2) == cudaSuccess &&
               cudaMalloc(&g.WbT, (size_t)H * H * 2) == cudaSuccess &&
-              cudaMalloc(&g.part, (size_t)g.splits * H * imax * 4) == cudaSuccess;
+              cudaMalloc(&g.part, (size_t)g.splits * std::max(H, t->nout_pad) * imax * 4) == cudaSuccess;
     for (int l = 0; l <= t->L && ok; ++l) {
         ok &= cudaMalloc(&g.gW[l], (size_t)t->out[l] * t->in[l] * 4) == cudaSuccess;
         ok &= cudaMalloc(&g.gb[l], (size_t)t->out[l] * 4) == cudaSuccess;
@@ -741,8 +772,14 @@ void step_gradients(const ves_shiftnet *t, int batch, const ves::bf16 *Xb, const
     forward(t, batch, Xb, a, err, st, true);
     ves::chamfer_kernel<<<ves::nb(batch, 128), 128, 0, st>>>(batch, n, t->nout_pad, a.Y, Tb, g.dA, loss, t->cfg.loss,
                                                              t->cfg.delta);
-    ves::dw_kernel<float><<<dim3(ves::nb(H, 128), t->nout_pad), 128, 0, st>>>(batch, t->nout_pad, H, g.dA, a.Hf, H,
-                                                                             g.gW[L], g.gb[L]);
+    {  // output layer: dW = dY^T Hf (FP32, split over the batch), db = column sums of dY
+        const int kz = (batch + g.splits - 1) / g.splits;
+        ves::sgemm_tn_splitk_kernel<<<dim3(ves::nb(H, 32), ves::nb(t->nout_pad, 32), g.splits), dim3(32, 8), 0, st>>>(
+            t->nout_pad, H, batch, g.dA, t->nout_pad, a.Hf, H, g.part, kz);
+        const long long nw = (long long)t->nout_pad * H;
+        ves::sum_splits_kernel<<<ves::nb(nw), 256, 0, st>>>(nw, g.splits, nw, g.part, g.gW[L]);
+        ves::colsum_kernel<<<ves::nb(t->nout_pad, 32), dim3(32, 32), 0, st>>>(batch, t->nout_pad, g.dA, g.gb[L]);
+    }
     ves::dh_kernel<<<dim3(ves::nb(H, 128), batch), 128, 0, st>>>(batch, t->nout_pad, H, g.dA, t->W[L], g.dB);
     ves::gelu_bwd_kernel<<<ves::nb((long long)batch * H), 256, 0, st>>>((long long)batch * H, g.dB, a.Z[L - 1], g.dB);
     float *dZ = g.dB, *dH = g.dA;
@@ -758,7 +795,7 @@ void step_gradients(const ves_shiftnet *t, int batch, const ves::bf16 *Xb, const
         ves::launch_gemm_bf16_splitk(H, in, batch, g.dZt, batch, g.HinT, batch, g.part, in, g.splits, err, st);
         ves::sum_splits_kernel<<<ves::nb((long long)H * in), 256, 0, st>>>((long long)H * in, g.splits,
                                                                           (long long)H * in, g.part, g.gW[l]);
-        ves::colsum_kernel<<<ves::nb(H, 128), 128, 0, st>>>(batch, H, dZ, g.gb[l]);
+        ves::colsum_kernel<<<ves::nb(H, 32), dim3(32, 32), 0, st>>>(batch, H, dZ, g.gb[l]);
         if (l > 0) {
             ves::to_bf16_kernel<<<ves::nb(nz), 256, 0, st>>>(nz, dZ, g.dZ16);
             ves::transpose_bf16_kernel<ves::bf16><<<dim3(ves::nb(H, 32), ves::nb(H, 32)), tb, 0, st>>>(
@@ -841,16 +878,16 @@ int ves_shiftnet_train(ves_shiftnet *t, long long count, int thread_cnt, const d
         const Acts a = carve_acts(t, batch, w);
         cudaMemsetAsync(err, 0, 4, st);
         // standardisation statistics over the whole training set
-        ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, t->P, t->F, t->S, thread_cnt, params, rA, iA,
+        ves::features_kernel<<<ves::nb(count * 32, 256), 256, 0, st>>>(count, n, t->P, t->F, t->S, thread_cnt, params, rA, iA,
                                                              nullptr, nullptr, t->kin, t->kin_pad, Xall, nullptr);
         ves::colstats_bf16_kernel<<<ves::nb(t->kin_pad), 256, 0, st>>>(count, t->kin_pad, t->kin_pad, Xall, t->fmean,
                                                                       t->fstd);
-        ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, t->P, t->F, t->S, thread_cnt, params, rA, iA,
+        ves::features_kernel<<<ves::nb(count * 32, 256), 256, 0, st>>>(count, n, t->P, t->F, t->S, thread_cnt, params, rA, iA,
                                                              t->fmean, t->fstd, t->kin, t->kin_pad, Xall, nullptr);
-        ves::targets_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, thread_cnt, rE, iE, nullptr, nullptr,
+        ves::targets_kernel<<<ves::nb(count * 32, 256), 256, 0, st>>>(count, n, thread_cnt, rE, iE, nullptr, nullptr,
                                                             t->nout_pad, Tall, nullptr);
         ves::target_stats_kernel<<<1, 256, 0, st>>>(count, n, t->nout_pad, t->nout_pad, Tall, t->tmean, t->tstd);
-        ves::targets_kernel<<<ves::nb(count), 256, 0, st>>>(count, n, thread_cnt, rE, iE, t->tmean, t->tstd,
+        ves::targets_kernel<<<ves::nb(count * 32, 256), 256, 0, st>>>(count, n, thread_cnt, rE, iE, t->tmean, t->tstd,
                                                             t->nout_pad, Tall, nullptr);
         std::mt19937_64 rng(seed);
         std::vector<int> perm(count);
@@ -865,10 +902,10 @@ int ves_shiftnet_train(ves_shiftnet *t, long long count, int thread_cnt, const d
             cudaMemsetAsync(loss, 0, 4, st);
             for (long long s = 0; s < steps_per_epoch; ++s) {
                 const int *r = rows + s * batch;
-                ves::features_kernel<<<ves::nb(batch), 256, 0, st>>>(batch, n, t->P, t->F, t->S, thread_cnt, params,
+                ves::features_kernel<<<ves::nb(batch * 32, 256), 256, 0, st>>>(batch, n, t->P, t->F, t->S, thread_cnt, params,
                                                                      rA, iA, t->fmean, t->fstd, t->kin, t->kin_pad,
                                                                      Xb, r);
-                ves::targets_kernel<<<ves::nb(batch), 256, 0, st>>>(batch, n, thread_cnt, rE, iE, t->tmean, t->tstd,
+                ves::targets_kernel<<<ves::nb(batch * 32, 256), 256, 0, st>>>(batch, n, thread_cnt, rE, iE, t->tmean, t->tstd,
                                                                     t->nout_pad, Tb, r);
                 step_gradients(t, batch, Xb, Tb, a, g, loss, err, st);
                 ++t->step;
@@ -934,9 +971,9 @@ int ves_shiftnet_gradient(const ves_shiftnet *t, long long count, int thread_cnt
         const Acts a = carve_acts(t, batch, w);
         cudaMemsetAsync(err, 0, 4, st);
         cudaMemsetAsync(loss, 0, 4, st);
-        ves::features_kernel<<<ves::nb(batch), 256, 0, st>>>(batch, t->n, t->P, t->F, t->S, thread_cnt, params, rA, iA,
+        ves::features_kernel<<<ves::nb(batch * 32, 256), 256, 0, st>>>(batch, t->n, t->P, t->F, t->S, thread_cnt, params, rA, iA,
                                                              t->fmean, t->fstd, t->kin, t->kin_pad, X, nullptr);
-        ves::targets_kernel<<<ves::nb(batch), 256, 0, st>>>(batch, t->n, thread_cnt, rE, iE, t->tmean, t->tstd,
+        ves::targets_kernel<<<ves::nb(batch * 32, 256), 256, 0, st>>>(batch, t->n, thread_cnt, rE, iE, t->tmean, t->tstd,
                                                             t->nout_pad, T, nullptr);
         step_gradients(t, batch, X, T, a, g, loss, err, st);
         size_t off = 0;
@@ -983,7 +1020,7 @@ int ves_shiftnet_predict(const ves_shiftnet *t, long long count, int thread_cnt,
     w += ((size_t)count * t->kin_pad * 2 + 255) & ~(size_t)255;
     const Acts a = carve_acts(t, (size_t)count, w);
     int *err = nullptr;  // a GEMM wait that gives up leaves its tile unwritten; training checks the flag
-    ves::features_kernel<<<ves::nb(count), 256, 0, st>>>(count, t->n, t->P, t->F, t->S, thread_cnt, params, rA, iA,
+    ves::features_kernel<<<ves::nb(count * 32, 256), 256, 0, st>>>(count, t->n, t->P, t->F, t->S, thread_cnt, params, rA, iA,
                                                          t->fmean, t->fstd, t->kin, t->kin_pad, X, nullptr);
     if (forward(t, (int)count, X, a, err, st, false) != cudaSuccess) return fail(VES_ERR_CUDA, "shiftnet predict: launch failed");
     ves::shifts_out_kernel<<<ves::nb(count), 256, 0, st>>>(count, t->n, thread_cnt, t->nout_pad, a.Y, t->tmean,
