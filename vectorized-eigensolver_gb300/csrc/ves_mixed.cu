@@ -457,6 +457,7 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
 {
     extern __shared__ float2 gsm[];
     constexpr int MPW = 32 / G;  // matrices per warp
+    constexpr int NPL = 16 / G;  // rows (columns) of an update per lane, n <= 16
     const int n = a.g.n, tc = a.g.tc;
     const int lane = threadIdx.x & 31, gl = lane & (G - 1), j0 = gl + 1;
     const unsigned gmask = group_mask<G>(lane);
@@ -629,28 +630,49 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
                 if (act && K > L && gl == 0) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(0.f, 0.f)); }
                 const cx<float> w1 = a1, cw = conj(w1), c1 = conj(t1);
                 const float t2 = fmaf(t1.r, w1.r, -(t1.i * w1.i));
+                // A lane's share of a step, n <= 16: at most NPL rows and columns;
+                // the loops have a fixed trip count with predicated elements, so all
+                // of a lane's loads issue before its rotations (independent chains).
                 if (act) {
-                    for (int j = K + gl; j <= n; j += G) {  // rows K, K+1, columns K..n
-                        cx<float> h1 = H.ld(K, j), h2 = H.ld(K + 1, j);
-                        rot_pair(h1, h2, c1, t2, w1);
-                        H.st(K, j, h1);
-                        H.st(K + 1, j, h2);
+                    cx<float> h1[NPL], h2[NPL], z1[NPL], z2[NPL];
+#pragma unroll
+                    for (int t = 0; t < NPL; ++t) {
+                        const int jr = K + gl + t * G, jz = j0 + t * G;
+                        if (jr <= n) { h1[t] = H.ld(K, jr); h2[t] = H.ld(K + 1, jr); }  // rows K, K+1, columns K..n
+                        if (jz <= n) { z1[t] = Z.ld(jz, K); z2[t] = Z.ld(jz, K + 1); }  // Schur vectors: columns K, K+1
                     }
-                    for (int j = j0; j <= n; j += G) {  // Schur vectors: columns K, K+1
-                        cx<float> z1 = Z.ld(j, K), z2 = Z.ld(j, K + 1);
-                        rot_pair(z1, z2, t1, t2, cw);
-                        Z.st(j, K, z1);
-                        Z.st(j, K + 1, z2);
+#pragma unroll
+                    for (int t = 0; t < NPL; ++t) {
+                        const int jr = K + gl + t * G, jz = j0 + t * G;
+                        if (jr <= n) {
+                            rot_pair(h1[t], h2[t], c1, t2, w1);
+                            H.st(K, jr, h1[t]);
+                            H.st(K + 1, jr, h2[t]);
+                        }
+                        if (jz <= n) {
+                            rot_pair(z1[t], z2[t], t1, t2, cw);
+                            Z.st(jz, K, z1[t]);
+                            Z.st(jz, K + 1, z2[t]);
+                        }
                     }
                 }
                 __syncwarp();  // the row update is done: the column update shares the 2 x 2 block
                 if (act) {
-                    const int je = (K + 2) < I ? (K + 2) : I;
-                    for (int j = j0; j <= je; j += G) {  // columns K, K+1, rows 1..min(K+2, I)
-                        cx<float> h1 = H.ld(j, K), h2 = H.ld(j, K + 1);
-                        rot_pair(h1, h2, t1, t2, cw);
-                        H.st(j, K, h1);
-                        H.st(j, K + 1, h2);
+                    const int je = (K + 2) < I ? (K + 2) : I;  // columns K, K+1, rows 1..min(K+2, I)
+                    cx<float> h1[NPL], h2[NPL];
+#pragma unroll
+                    for (int t = 0; t < NPL; ++t) {
+                        const int j = j0 + t * G;
+                        if (j <= je) { h1[t] = H.ld(j, K); h2[t] = H.ld(j, K + 1); }
+                    }
+#pragma unroll
+                    for (int t = 0; t < NPL; ++t) {
+                        const int j = j0 + t * G;
+                        if (j <= je) {
+                            rot_pair(h1[t], h2[t], t1, t2, cw);
+                            H.st(j, K, h1[t]);
+                            H.st(j, K + 1, h2[t]);
+                        }
                     }
                 }
                 __syncwarp();
@@ -961,9 +983,11 @@ namespace {
 // on GB300 (FP32+refine eigensolves/s, stages in sequence, two float-float
 // steps): n=8 lane 47.9, group4 43.0, group8 36.1 M/s; n=12 lane 14.4,
 // group4 15.4, group8 12.9 M/s; n=16 lane 6.10 (6.43 overlapped), group4
-// 6.78, group8 7.04 M/s.  Default: the group kernel with G = 4 for
-// 11 <= n <= 13 and G = 8 for 14 <= n <= 16.  Older measurements, before the
-// fast FP32 arithmetic and the group kernels:  Measured on GB300,
+// 6.78, group8 7.04 M/s; later, with the division-free FP64 deflation test
+// and unrolled lane shares: n=11 lane 17.95, group4 19.88, group8 16.44;
+// n=14 8.72, 10.64, 10.16; n=16 5.95, 7.23, 7.72 M/s.  Default: the group
+// kernel with G = 4 for 11 <= n <= 14 and G = 8 for n = 15, 16.  Older
+// measurements, before the fast FP32 arithmetic and the group kernels:  Measured on GB300,
 // FP32+refine eigensolves/s, lane -> warp (G = 32): n=16 5.34 -> 4.26 M/s,
 // n=24 1.59 -> 1.63 M/s, n=32 0.66 -> 0.72 M/s (below 24 too many lanes of a
 // warp idle).  Two matrices per warp (G = 16) does not recover it: with the
@@ -983,8 +1007,8 @@ int schur_group(int n)
     if (e && !strcmp(e, "warp32")) return n <= 32 ? 32 : 0;
     if (e && !strcmp(e, "group4")) return n <= 16 ? 4 : 0;
     if (e && !strcmp(e, "group8")) return n <= 16 ? 8 : 0;
-    if (n >= 11 && n <= 13) return 4;
-    if (n >= 14 && n <= 16) return 8;
+    if (n >= 11 && n <= 14) return 4;
+    if (n >= 15 && n <= 16) return 8;
     return (n >= 24 && n <= 32) ? 32 : 0;
 }
 
