@@ -520,22 +520,56 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
                 if (k >= i + 2) H.st(k, i, cmul(H.ld(k, i), scale));
             if (gl == 0) sTau[i - 1] = make_float2(t.r, t.i);
             __syncwarp(gmask);
-            for (int r = j0; r <= n; r += G) {  // right: row r of A(1:n, i+1:n) -= tau (A v)_r v^H
-                cx<float> sacc = H.ld(r, i + 1);
-                for (int q = 2; q <= mm; ++q) sacc = cmac(sacc, H.ld(r, i + q), H.ld(i + q, i));
-                const cx<float> ts = cmul(t, sacc);
-                H.st(r, i + 1, csub(H.ld(r, i + 1), ts));
-                for (int q = 2; q <= mm; ++q) H.st(r, i + q, cnmacc(H.ld(r, i + q), ts, H.ld(i + q, i)));
+            // the lane's rows (columns) side by side: NPL independent dot-product chains
+            {  // right: row r of A(1:n, i+1:n) -= tau (A v)_r v^H
+                cx<float> sacc[NPL];
+#pragma unroll
+                for (int u = 0; u < NPL; ++u) {
+                    const int r = j0 + u * G;
+                    if (r <= n) sacc[u] = H.ld(r, i + 1);
+                }
+                for (int q = 2; q <= mm; ++q) {
+                    const cx<float> vq = H.ld(i + q, i);
+#pragma unroll
+                    for (int u = 0; u < NPL; ++u) {
+                        const int r = j0 + u * G;
+                        if (r <= n) sacc[u] = cmac(sacc[u], H.ld(r, i + q), vq);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < NPL; ++u) {
+                    const int r = j0 + u * G;
+                    if (r > n) continue;
+                    const cx<float> ts = cmul(t, sacc[u]);
+                    H.st(r, i + 1, csub(H.ld(r, i + 1), ts));
+                    for (int q = 2; q <= mm; ++q) H.st(r, i + q, cnmacc(H.ld(r, i + q), ts, H.ld(i + q, i)));
+                }
             }
             __syncwarp(gmask);
             const cx<float> tcj = conj(t);
-            for (int c = j0; c <= n; c += G) {  // left: column c of A(i+1:n, i+1:n) -= conj(tau) v (v^H A)_c
-                if (c < i + 1) continue;
-                cx<float> sacc = H.ld(i + 1, c);
-                for (int q = 2; q <= mm; ++q) sacc = cjmac(sacc, H.ld(i + q, i), H.ld(i + q, c));
-                const cx<float> ts = cmul(tcj, sacc);
-                H.st(i + 1, c, csub(H.ld(i + 1, c), ts));
-                for (int q = 2; q <= mm; ++q) H.st(i + q, c, cnmac(H.ld(i + q, c), H.ld(i + q, i), ts));
+            {  // left: column c of A(i+1:n, i+1:n) -= conj(tau) v (v^H A)_c
+                cx<float> sacc[NPL];
+#pragma unroll
+                for (int u = 0; u < NPL; ++u) {
+                    const int c = j0 + u * G;
+                    if (c >= i + 1 && c <= n) sacc[u] = H.ld(i + 1, c);
+                }
+                for (int q = 2; q <= mm; ++q) {
+                    const cx<float> vq = H.ld(i + q, i);
+#pragma unroll
+                    for (int u = 0; u < NPL; ++u) {
+                        const int c = j0 + u * G;
+                        if (c >= i + 1 && c <= n) sacc[u] = cjmac(sacc[u], vq, H.ld(i + q, c));
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < NPL; ++u) {
+                    const int c = j0 + u * G;
+                    if (c < i + 1 || c > n) continue;
+                    const cx<float> ts = cmul(tcj, sacc[u]);
+                    H.st(i + 1, c, csub(H.ld(i + 1, c), ts));
+                    for (int q = 2; q <= mm; ++q) H.st(i + q, c, cnmac(H.ld(i + q, c), H.ld(i + q, i), ts));
+                }
             }
             __syncwarp(gmask);
             if (gl == 0) H.st(i + 1, i, mk(beta, 0.f));
@@ -547,13 +581,29 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
         for (int i = n - 1; i >= 1; --i) {
             const cx<float> t = mk(sTau[i - 1].x, sTau[i - 1].y);
             const int c = i + 1;
-            for (int j = j0; j <= n; j += G) {
-                if (j < c + 1) continue;
-                cx<float> sacc = Z.ld(c, j);
-                for (int k = c + 1; k <= n; ++k) sacc = cjmac(sacc, H.ld(k, i), Z.ld(k, j));
-                const cx<float> ts = cmul(t, sacc);
-                Z.st(c, j, csub(Z.ld(c, j), ts));
-                for (int k = c + 1; k <= n; ++k) Z.st(k, j, cnmac(Z.ld(k, j), H.ld(k, i), ts));
+            {
+                cx<float> sacc[NPL];
+#pragma unroll
+                for (int u = 0; u < NPL; ++u) {
+                    const int j = j0 + u * G;
+                    if (j >= c + 1 && j <= n) sacc[u] = Z.ld(c, j);
+                }
+                for (int k = c + 1; k <= n; ++k) {
+                    const cx<float> hk = H.ld(k, i);
+#pragma unroll
+                    for (int u = 0; u < NPL; ++u) {
+                        const int j = j0 + u * G;
+                        if (j >= c + 1 && j <= n) sacc[u] = cjmac(sacc[u], hk, Z.ld(k, j));
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < NPL; ++u) {
+                    const int j = j0 + u * G;
+                    if (j < c + 1 || j > n) continue;
+                    const cx<float> ts = cmul(t, sacc[u]);
+                    Z.st(c, j, csub(Z.ld(c, j), ts));
+                    for (int k = c + 1; k <= n; ++k) Z.st(k, j, cnmac(Z.ld(k, j), H.ld(k, i), ts));
+                }
             }
             __syncwarp(gmask);
             for (int j = j0; j <= n; j += G) {
