@@ -949,6 +949,16 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(const MixedArgs 
         refine_tile<MAXN, kPerMatrix>(a, buf, flags, tile);
 }
 
+// The same for n <= 16 after the lane Schur kernel (n <= 10 by default), held
+// to 64 registers for 16 resident blocks per SM: n=8 measured 49.0 -> 51.4 M/s;
+// the same bound on the per-matrix instances cost 2-4% at n=16 and 32.
+__global__ void __launch_bounds__(kRefineThreads, 16) refine16_lane_kernel(const MixedArgs a, const float2 *buf,
+                                                                           int *flags)
+{
+    const long long ntiles = ((a.m_end - a.m_begin) * a.g.n + kRefineThreads - 1) / kRefineThreads;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) refine_tile<16, false>(a, buf, flags, tile);
+}
+
 // Distinctness of the refined eigenvalues of each matrix.  Newton from two
 // FP32 starting points can land on the same eigenpair when the FP32 Schur
 // form does not resolve a cluster: both pairs pass their residual and
@@ -1158,7 +1168,7 @@ cudaError_t launch_refine(const MixedArgs &a, cudaStream_t st)
         else
             refine_kernel<32, true><<<rb, kRefineThreads, 0, st>>>(a, b.buf, b.flags);
     } else if (n <= 16) {
-        refine_kernel<16, false><<<rb, kRefineThreads, 0, st>>>(a, b.buf, b.flags);
+        refine16_lane_kernel<<<rb, kRefineThreads, 0, st>>>(a, b.buf, b.flags);
     } else if (n <= 32) {
         refine_kernel<32, false><<<rb, kRefineThreads, 0, st>>>(a, b.buf, b.flags);
     } else {
@@ -1275,7 +1285,7 @@ cudaError_t launch_mixed_overlap(const MixedArgs &a0, cudaStream_t st, cudaStrea
 void load_mixed_kernels()
 {
     load_kernel(schur32_kernel);
-    load_kernel(refine_kernel<16, false>);
+    load_kernel(refine16_lane_kernel);
     load_kernel(refine_kernel<32, false>);
     load_kernel(refine_kernel<64, false>);
     load_kernel(schur32_warp_kernel<32>);
