@@ -676,8 +676,9 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
                     if (K > L) { a0 = H.ld(K, K - 1); a1 = H.ld(K + 1, K - 1); }
                     zlarfg2<float>(a0, a1, t1);
                 }
-                __syncwarp();  // every lane has read H(K, K-1), H(K+1, K-1)
-                if (act && K > L && gl == 0) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(0.f, 0.f)); }
+                // (the reflector's entries in column K-1 are stored after the next
+                // synchronisation: the row update below does not touch that column,
+                // so no lane can still be reading them then)
                 const cx<float> w1 = a1, cw = conj(w1), c1 = conj(t1);
                 const float t2 = fmaf(t1.r, w1.r, -(t1.i * w1.i));
                 // A lane's share of a step, n <= 16: at most NPL rows and columns;
@@ -707,6 +708,7 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
                     }
                 }
                 __syncwarp();  // the row update is done: the column update shares the 2 x 2 block
+                if (act && K > L && gl == 0) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(0.f, 0.f)); }
                 if (act) {
                     const int je = (K + 2) < I ? (K + 2) : I;  // columns K, K+1, rows 1..min(K+2, I)
                     cx<float> h1[NPL], h2[NPL];
@@ -734,7 +736,10 @@ __global__ void __launch_bounds__(kGroupSchurThreads) schur32_group_kernel(const
                 const float d = cabs(h);
                 const cx<float> z = conj(cscal(h, frcp<float>(d)));
                 if (gl == 0) H.st(I, I - 1, mk(d, 0.f));
-                for (int j = j0; j <= n; j += G) {
+#pragma unroll
+                for (int t = 0; t < NPL; ++t) {
+                    const int j = j0 + t * G;
+                    if (j > n) continue;
                     if (j >= I + 1) H.st(I, j, cmul(H.ld(I, j), z));
                     if (j <= I - 1) H.st(j, I, cmulc(H.ld(j, I), z));
                     Z.st(j, I, cmulc(Z.ld(j, I), z));
