@@ -332,8 +332,6 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
                     cx<float> a0 = v0, a1 = v1, t1;
                     if (K > L) { a0 = H.ld(K, K - 1); a1 = H.ld(K + 1, K - 1); }
                     zlarfg2<float>(a0, a1, t1);
-                    __syncwarp(gmask);
-                    if (K > L && gl == 0) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(0.f, 0.f)); }
                     const cx<float> w1 = a1, cw = conj(w1), c1 = conj(t1);
                     const float t2 = fmaf(t1.r, w1.r, -(t1.i * w1.i));
                     if (j >= K && j <= n) {  // rows K, K+1, column j
@@ -343,6 +341,9 @@ __global__ void __launch_bounds__(kWarpSchurThreads) schur32_warp_kernel(const M
                         H.st(K + 1, j, h2);
                     }
                     __syncwarp(gmask);
+                    // the reflector's entries in column K-1, stored once every lane has
+                    // read them (the row update above does not touch that column)
+                    if (K > L && gl == 0) { H.st(K, K - 1, a0); H.st(K + 1, K - 1, mk(0.f, 0.f)); }
                     const int je = (K + 2) < I ? (K + 2) : I;
                     if (j <= je) {  // columns K, K+1, row j
                         cx<float> h1 = H.ld(j, K), h2 = H.ld(j, K + 1);
