@@ -170,7 +170,7 @@ def test_fullsize_learned_config():
     st = torch.full((N,), -1, dtype=torch.int32, device="cuda")
     sw = torch.zeros(N, dtype=torch.int32, device="cuda")
     ves.eigensolve_shifts(n, N // TC, TC, rA, iA, rE, iE, rV, iV, rS, iS, status=st, sweeps=sw,
-                          options=ves.default_options(shift_polish=6, shift_gate=3e-2))
+                          options=ves.default_options(shift_polish=16, shift_gate=0.0))
     torch.cuda.synchronize()
     assert int(((st & ~ves.VES_STATUS_SHIFT_FALLBACK) != 0).sum()) == 0
     A = soa_planes_to_batch(rA, iA, n, TC)

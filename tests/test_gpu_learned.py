@@ -136,3 +136,43 @@ def test_polish_recovers_noisy_predictions(n):
     assert (err / nA).max() <= 1e-12
     assert sw.double().mean().item() < 0.8 * sw0.double().mean().item()
     assert ((st & ~ves.VES_STATUS_SHIFT_FALLBACK) == 0).all()
+
+
+@pytest.mark.parametrize("n", [16, 40])
+def test_polish_separates_duplicate_predictions(n):
+    """Predictions in coinciding pairs (the prediction of every odd-numbered
+    eigenvalue replaced by its neighbour's, 1e-3 apart): the Aberth polish
+    pushes one of each pair to the eigenvalue that has no prediction, so the
+    QR needs fewer sweeps than when every prediction is polished on its own
+    (Newton, the n <= 32 pre-pass's VES_POLISH_METHOD=newton); the result
+    meets the plain solver's bar either way."""
+    import torch
+    N = 4096
+    p, rA, iA = learned_shift.family(N, n, param_seed=15)
+    rE0, iE0, sw0 = learned_shift.solve_plain(n, N, rA, iA, TC)
+    g = torch.Generator(device="cuda").manual_seed(2)
+    rS = rE0 + 1e-2 * torch.randn(rE0.shape, generator=g, device="cuda", dtype=torch.float64)
+    iS = iE0 + 1e-2 * torch.randn(rE0.shape, generator=g, device="cuda", dtype=torch.float64)
+    for P in (rS, iS):
+        v = P.view(N // TC, n, TC)
+        v[:, 1::2, :] = v[:, 0:n - 1:2, :] + 1e-3
+    E0 = ves.complex_vec_from_soa(rE0.cpu().numpy(), iE0.cpu().numpy(), n, TC)
+    nA = np.linalg.norm(ves.complex_from_soa(rA.cpu().numpy(), iA.cpu().numpy(), n, TC), axis=(1, 2))
+    sweeps = {}
+    for method in (["aberth", "newton"] if n <= 32 else ["aberth"]):
+        os.environ["VES_POLISH_METHOD"] = method
+        try:
+            rE, iE, st, sw, fb, res = solve_shifts(n, N, rA, iA, rS, iS, shift_polish=16)
+        finally:
+            del os.environ["VES_POLISH_METHOD"]
+        assert res <= 1e-13
+        E = ves.complex_vec_from_soa(rE.cpu().numpy(), iE.cpu().numpy(), n, TC)
+        _, err, _ = match_eigs(E, E0)
+        assert (err / nA).max() <= 1e-12
+        assert ((st & ~ves.VES_STATUS_SHIFT_FALLBACK) == 0).all()
+        sweeps[method] = sw.double().mean().item()
+    plain = sw0.double().mean().item()
+    print("sweeps per matrix: plain %.2f, %s" % (plain, sweeps))
+    assert sweeps["aberth"] < 0.8 * plain
+    if "newton" in sweeps:
+        assert sweeps["aberth"] < 0.95 * sweeps["newton"]

@@ -892,7 +892,7 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *
     if (opt) o = *opt;
     if (o.max_its < 0 || o.max_its > 10000 || o.vnorm < 0 || o.vnorm > 2 || o.shift_sweeps < 0 ||
         o.shift_sweeps > 9 || o.blocks_per_sm < 0 || o.blocks_per_sm > 16 || !(o.shift_gate >= 0.f) ||
-        o.shift_gate > 1e6f || o.shift_polish < 0 || o.shift_polish > 16) {
+        o.shift_gate > 1e6f || o.shift_polish < 0 || o.shift_polish > 64) {
         set_error("option out of range");
         return VES_ERR_ARG;
     }

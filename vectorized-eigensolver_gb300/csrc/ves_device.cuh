@@ -752,33 +752,45 @@ struct ShiftPredictions {
     __device__ __forceinline__ void deflated(int its) { if (current >= 0 && its > sweeps + 2) ++fallbacks; }
 };
 
-// Newton's method on det(H - s I) for the upper Hessenberg H, in FP32 on Hf
-// (an FP32 copy of H), by Hyman's recurrence: with x_n = 1,
+// Polish of the predicted shifts: simultaneous (Aberth-Ehrlich) iteration on
+// det(H - s I) for the upper Hessenberg H, in FP32 on Hf (an FP32 copy of H).
+// Hyman's recurrence gives the Newton correction N = p(s) / p'(s): with x_n = 1,
 //     x_{i-1} = -[(h_ii - s) x_i + sum_{j>i} h_ij x_j] / h_{i,i-1},   i = n..2,
 //     r(s)    = (h_11 - s) x_1 + sum_{j>1} h_1j x_j,
-// det(H - s I) = c r(s) with c independent of s, so a Newton step is r / r',
-// r' from the differentiated recurrence (x, x' are rescaled together when
-// they grow: the ratio does not depend on their common scale).  Each
-// prediction in S gets up to `steps` steps, stopping once a step is below
-// `tol`.  A prediction is kept only if its last step was below `keep` (the
-// iteration has reached its quadratic phase): one that has not converged, or
-// whose iteration broke down (a zero subdiagonal, non-finite values), or that
-// lands within `dup` of an earlier one is dropped (NaN), and its eigenvalue is
-// found with the Wilkinson shift -- a far prediction costs sweeps, a dropped
-// one costs nothing.  The FP32 pipe does this work at a small fraction of one
-// FP64 QR sweep.
+// det(H - s I) = c r(s) with c independent of s, so N = r / r', r' from the
+// differentiated recurrence (x, x' are rescaled together when they grow: the
+// ratio does not depend on their common scale).  Aberth's step is Newton's on
+// p(s) / prod_{q != k} (s - s_q): s_k -= N / (1 - N sum_{q != k} 1/(s_k - s_q)),
+// which pushes two predictions near one eigenvalue apart instead of letting
+// both converge to it (Aberth 1973, Ehrlich 1967).  Here the sweep over the
+// predictions uses the newest values (Gauss-Seidel order).  Each prediction
+// in S takes up to `steps` steps, stopping once a step is below `tol`; it is
+// kept only if its last step was below `keep` (the iteration has reached its
+// fast phase): one that has not converged, or whose iteration broke down (a
+// zero subdiagonal, non-finite values), or that lands within `dup` of an
+// earlier one is dropped (NaN), and its eigenvalue is found with the
+// Wilkinson shift -- a far prediction costs sweeps, a dropped one costs
+// nothing.  The FP32 pipe does this work at a small fraction of one FP64 QR
+// sweep.
 template <int MAXN>
 __device__ void polish_shifts_lane(const int n, const MatIlv<float> &Hf, const VecIlv<double> &S, const int steps,
                                    const float tol, const float keep, const float dup)
 {
+    static_assert(MAXN <= 64, "one bit per prediction");
     const double nan = __longlong_as_double(0x7ff8000000000000LL);
     cx<float> x[MAXN], dx[MAXN];
+    unsigned long long live = 0, done = 0, good = 0;
     for (int k = 1; k <= n; ++k) {
         const cx<double> s0 = S.ld(k);
-        cx<float> s = mk((float)s0.r, (float)s0.i);
-        bool ok = !nonfinite(s.r) && !nonfinite(s.i) && n >= 2;
-        float last = 3.0e38f;
-        for (int it = 0; it < steps && ok; ++it) {
+        if (!nonfinite(s0.r) && !nonfinite(s0.i) && n >= 2) live |= 1ULL << (k - 1);
+    }
+    for (int it = 0; it < steps && (live & ~done); ++it) {
+        for (int k = 1; k <= n; ++k) {
+            const unsigned long long bit = 1ULL << (k - 1);
+            if (!(live & bit) || (done & bit)) continue;
+            const cx<double> s0 = S.ld(k);
+            const cx<float> s = mk((float)s0.r, (float)s0.i);
+            bool ok = true;
             x[n - 1] = mk(1.f, 0.f);
             dx[n - 1] = mk(0.f, 0.f);
             for (int i = n; i >= 2; --i) {
@@ -798,23 +810,38 @@ __device__ void polish_shifts_lane(const int n, const MatIlv<float> &Hf, const V
                     for (int j = i - 1; j <= n; ++j) { x[j - 1] = cscal(x[j - 1], 1e-18f); dx[j - 1] = cscal(dx[j - 1], 1e-18f); }
                 }
             }
-            if (!ok) break;
-            const cx<float> d1 = csub(Hf.ld(1, 1), s);
-            cx<float> r = cmul(d1, x[0]);
-            cx<float> rp = csub(cmul(d1, dx[0]), x[0]);
-            for (int j = 2; j <= n; ++j) {
-                const cx<float> h = Hf.ld(1, j);
-                r = cmac(r, h, x[j - 1]);
-                rp = cmac(rp, h, dx[j - 1]);
+            cx<float> delta = mk(0.f, 0.f);
+            if (ok) {
+                const cx<float> d1 = csub(Hf.ld(1, 1), s);
+                cx<float> r = cmul(d1, x[0]);
+                cx<float> rp = csub(cmul(d1, dx[0]), x[0]);
+                for (int j = 2; j <= n; ++j) {
+                    const cx<float> h = Hf.ld(1, j);
+                    r = cmac(r, h, x[j - 1]);
+                    rp = cmac(rp, h, dx[j - 1]);
+                }
+                delta = cdiv(r, rp);
+                ok = !nonfinite(delta.r) && !nonfinite(delta.i);
             }
-            const cx<float> delta = cdiv(r, rp);
-            if (nonfinite(delta.r) || nonfinite(delta.i)) { ok = false; break; }
-            s = csub(s, delta);
-            last = cabs1(delta);
-            if (last <= tol) break;
+            if (!ok) { live &= ~bit; continue; }
+            cx<float> w = mk(0.f, 0.f);
+            for (int q = 1; q <= n; ++q) {
+                if (q == k || !(live & (1ULL << (q - 1)))) continue;
+                const cx<double> sq = S.ld(q);
+                const cx<float> d = mk(s.r - (float)sq.r, s.i - (float)sq.i);
+                if (d.r != 0.f || d.i != 0.f) w = cadd(w, cinv(d));
+            }
+            const cx<float> ab = cdiv(delta, csub(mk(1.f, 0.f), cmul(delta, w)));
+            if (!nonfinite(ab.r) && !nonfinite(ab.i)) delta = ab;
+            const cx<float> sn = csub(s, delta);
+            S.st(k, mk((double)sn.r, (double)sn.i));
+            const float last = cabs1(delta);
+            good = last <= keep ? (good | bit) : (good & ~bit);
+            if (last <= tol) done |= bit;
         }
-        S.st(k, ok && last <= keep ? mk((double)s.r, (double)s.i) : mk(nan, nan));
     }
+    for (int k = 1; k <= n; ++k)
+        if (!(live & good & (1ULL << (k - 1)))) S.st(k, mk(nan, nan));
     for (int k = 2; k <= n; ++k) {
         const cx<double> sk = S.ld(k);
         for (int j = 1; j < k; ++j) {

@@ -116,7 +116,7 @@ cudaError_t launch_backsubs(Geom g, const double *rT, const double *iT, double *
 cudaError_t launch_fused_fp64_blocks(const FusedArgs &a, int blocks, cudaStream_t st);
 
 // Learned-shift polish pre-pass (n <= 32): predictions (rS, iS) refined by
-// Newton steps on the FP32 Hessenberg form, written to (rP, iP); NaN = dropped.
+// Aberth steps on the FP32 Hessenberg form, written to (rP, iP); NaN = dropped.
 cudaError_t launch_polish32(Geom g, const double *rA, const double *iA, const double *rS, const double *iS,
                             double *rP, double *iP, int steps, unsigned long long *work, cudaStream_t st);
 

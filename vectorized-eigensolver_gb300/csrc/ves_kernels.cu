@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 
 namespace ves {
 
@@ -437,12 +438,15 @@ __global__ void __launch_bounds__(32) fp64_warp_kernel(const FusedArgs a)
 // Learned-shift polish pre-pass for n <= 32: one matrix per warp in shared
 // memory, FP32.  The warp reduces its matrix to Hessenberg form (hess32_warp;
 // FP32 rounding moves the eigenvalues by ~1e-7 relative, far below what the
-// shifts need), then lane k takes prediction k through up to `steps` Newton
-// steps on det(H - sI) by Hyman's recurrence (the iteration of
+// shifts need), then lane k takes prediction k through up to `steps` steps on
+// det(H - sI): the Newton correction by Hyman's recurrence (as in
 // polish_shifts_lane, with every lane's x and x' in shared memory and H read
-// as broadcasts), keeping it only if its last step was below 1e-3 of the
-// eigenvalue scale ||A||_F / sqrt(n) and no lower lane landed within 1e-5 of
-// it; dropped predictions are NaN.  Output: rP, iP in the SoA vector layout.
+// as broadcasts), turned into Aberth's correction with the other lanes'
+// current predictions (all lanes step together, Jacobi order; `aberth` = 0
+// keeps plain Newton).  A prediction is kept only if its last step was below
+// 1e-3 of the eigenvalue scale ||A||_F / sqrt(n) and no lower lane landed
+// within 1e-5 of it; dropped predictions are NaN.  Output: rP, iP in the SoA
+// vector layout.
 // ---------------------------------------------------------------------------
 constexpr int kPolishThreads = 128;  // 4 matrices per block
 
@@ -454,7 +458,8 @@ __host__ __device__ __forceinline__ size_t polish_warp_elems(int n)
 __global__ void __launch_bounds__(kPolishThreads) polish32_warp_kernel(const Geom g, const double *rA,
                                                                        const double *iA, const double *rS,
                                                                        const double *iS, double *rP, double *iP,
-                                                                       int steps, unsigned long long *work)
+                                                                       int steps, int aberth,
+                                                                       unsigned long long *work)
 {
     extern __shared__ float2 psm[];
     const int n = g.n, tc = g.tc;
@@ -539,8 +544,22 @@ __global__ void __launch_bounds__(kPolishThreads) polish32_warp_kernel(const Geo
                 r = cmac(r, h, mk(xq.x, xq.y));
                 rp = cmac(rp, h, mk(dxq.x, dxq.y));
             }
+            cx<float> delta = act ? cdiv(r, rp) : mk(0.f, 0.f);
+            if (aberth) {
+                // w = sum over the other live approximations s_q of 1 / (s - s_q),
+                // taken before any lane moves (all lanes step together)
+                const unsigned live = __ballot_sync(FULL, ok);
+                cx<float> w = mk(0.f, 0.f);
+                for (int q = 0; q < n; ++q) {
+                    const float qr = __shfl_sync(FULL, s.r, q), qi = __shfl_sync(FULL, s.i, q);
+                    const cx<float> d = mk(s.r - qr, s.i - qi);
+                    if (q != lane && ((live >> q) & 1u) && (d.r != 0.f || d.i != 0.f)) w = cadd(w, cinv(d));
+                }
+                // Aberth-Ehrlich: the Newton step on p(s) / prod_q (s - s_q)
+                const cx<float> ab = cdiv(delta, csub(mk(1.f, 0.f), cmul(delta, w)));
+                if (act && !nonfinite(ab.r) && !nonfinite(ab.i)) delta = ab;
+            }
             if (act) {
-                const cx<float> delta = cdiv(r, rp);
                 if (nonfinite(delta.r) || nonfinite(delta.i)) {
                     ok = false;
                 } else {
@@ -755,8 +774,12 @@ cudaError_t launch_polish32(Geom g, const double *rA, const double *iA, const do
                                                   polish_smem_bytes(g.n));
     const long long need = (g.N + kPolishThreads / 32 - 1) / (kPolishThreads / 32);
     const long long blocks = std::max<long long>(1, std::min<long long>(need, (long long)sms * std::max(per_sm, 1)));
+    // simultaneous (Aberth-Ehrlich) iteration by default; VES_POLISH_METHOD=newton
+    // polishes each prediction on its own (read per launch: cheap next to a solve)
+    const char *pm = getenv("VES_POLISH_METHOD");
+    const int aberth = (pm && strcmp(pm, "newton") == 0) ? 0 : 1;
     polish32_warp_kernel<<<(unsigned)blocks, kPolishThreads, polish_smem_bytes(g.n), st>>>(g, rA, iA, rS, iS, rP,
-                                                                                         iP, steps, work);
+                                                                                         iP, steps, aberth, work);
     return cudaGetLastError();
 }
 
