@@ -102,32 +102,53 @@ __device__ __forceinline__ void ff_mac(float &s, float &e, const float a, const 
     e = __fadd_rn(e, pe);
 }
 
+// One entry of an eigenvector iterate: float-float (head h, tail t with
+// |t| <= ulp(h) / 2) while the residuals are float-float, FP64 (d) from the
+// first FP64 residual on.  The two forms share the 16 bytes, so the per-lane
+// vector costs what an FP64 one does.
+union VEntry {
+    cx<double> d;
+    struct { cx<float> h, t; } f;
+};
+
+// (h, t) += s in float-float: TwoSum of the heads, the tail and the rounding
+// error summed, then renormalised (Fast2Sum, valid as |sum| >= |tail|).
+__device__ __forceinline__ void ff_add(float &h, float &t, const float s)
+{
+    const float sh = __fadd_rn(h, s);
+    const float bp = __fsub_rn(sh, h);
+    const float se = __fadd_rn(__fsub_rn(h, __fsub_rn(sh, bp)), __fsub_rn(s, bp));
+    const float tt = __fadd_rn(t, se);
+    h = __fadd_rn(sh, tt);
+    t = __fsub_rn(tt, __fsub_rn(h, sh));
+}
+
 // r = A v - lambda v in float-float on the FP32 pipe, into r32 (rounded to
-// FP32).  A = Ah + Al (two FP32 parts), v = vh + vl and lambda = lh + ll
-// (FP32 heads and tails; kLo = false: the tails are zero).  The head products
-// Ah vh and lh vh split exactly into rounded products and their errors (fma),
-// the rounded products are summed by TwoSum, and the errors, Ah vl, Al vh,
-// lh vl and ll vh are summed in FP32 beside them; Al vl and ll vl (~2^-48 of
-// the terms) are dropped.  Error ~ 2^-48 ||A|| ||v||.
+// FP32).  A = Ah + Al (two FP32 parts), v = vh + vl (the heads and tails of
+// v's float-float entries) and lambda = lh + ll (kLo = false: the tails are
+// zero).  The head products Ah vh and lh vh split exactly into rounded
+// products and their errors (fma), the rounded products are summed by TwoSum,
+// and the errors, Ah vl, Al vh, lh vl and ll vh are summed in FP32 beside
+// them; Al vl and ll vl (~2^-48 of the terms) are dropped.  Error ~ 2^-48
+// ||A|| ||v||.
 template <int MAXN, bool kLo, class MB>
-__device__ __forceinline__ void ff_residual(const int n, const MB &Ah, const MB &Al, const cx<float> *vh,
-                                            const cx<float> *vl, const cx<float> lh, const cx<float> ll,
-                                            cx<float> *r32)
+__device__ __forceinline__ void ff_residual(const int n, const MB &Ah, const MB &Al, const VEntry *v,
+                                            const cx<float> lh, const cx<float> ll, cx<float> *r32)
 {
     for (int i = 1; i <= n; ++i) {
-        const cx<float> vi = vh[i - 1];
+        const cx<float> vi = v[i - 1].f.h;
         float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f;
         ff_mac(sr, er, -lh.r, vi.r);
         ff_mac(sr, er, lh.i, vi.i);
         ff_mac(si, ei, -lh.r, vi.i);
         ff_mac(si, ei, -lh.i, vi.r);
         if (kLo) {
-            const cx<float> wi = vl[i - 1];
+            const cx<float> wi = v[i - 1].f.t;
             er = fmaf(lh.i, wi.i, fmaf(-lh.r, wi.r, fmaf(ll.i, vi.i, fmaf(-ll.r, vi.r, er))));
             ei = fmaf(-lh.i, wi.r, fmaf(-lh.r, wi.i, fmaf(-ll.i, vi.r, fmaf(-ll.r, vi.i, ei))));
         }
         for (int j = 1; j <= n; ++j) {
-            const cx<float> ah = Ah.ld(i, j), al = Al.ld(i, j), vj = vh[j - 1];
+            const cx<float> ah = Ah.ld(i, j), al = Al.ld(i, j), vj = v[j - 1].f.h;
             ff_mac(sr, er, ah.r, vj.r);
             ff_mac(sr, er, -ah.i, vj.i);
             ff_mac(si, ei, ah.r, vj.i);
@@ -135,7 +156,7 @@ __device__ __forceinline__ void ff_residual(const int n, const MB &Ah, const MB 
             er = fmaf(-al.i, vj.i, fmaf(al.r, vj.r, er));
             ei = fmaf(al.i, vj.r, fmaf(al.r, vj.i, ei));
             if (kLo) {
-                const cx<float> wj = vl[j - 1];
+                const cx<float> wj = v[j - 1].f.t;
                 er = fmaf(-ah.i, wj.i, fmaf(ah.r, wj.r, er));
                 ei = fmaf(ah.i, wj.r, fmaf(ah.r, wj.i, ei));
             }
@@ -816,16 +837,16 @@ __device__ __forceinline__ void refine_tile(const MixedArgs &a, const float2 *bu
     const long long mo = soa_off_m(m, nn, tc);
     const MatSoA<double> A{const_cast<double *>(a.rA) + mo, const_cast<double *>(a.iA) + mo, tc, n};
 
-    cx<double> v[MAXN];
-    cx<float> r32[MAXN], dx[MAXN], vl[MAXN];
+    VEntry v[MAXN];  // float-float up to the first FP64 residual, FP64 from there on
+    cx<float> r32[MAXN], dx[MAXN];
     cx<double> lam = mk(0.0, 0.0);
     if (act) {
         lam = up(T.ld(k, k));
         for (int i = 1; i <= n; ++i) {  // v = Z X(:,k), X upper triangular
             cx<float> acc = mk(0.f, 0.f);
             for (int j = 1; j <= k; ++j) acc = cmac(acc, Z.ld(i, j), X.ld(j, k));
-            v[i - 1] = up(acc);
-            dx[i - 1] = acc;  // v0 in FP32 for the first residual (dx is free until then)
+            v[i - 1].f.h = acc;
+            v[i - 1].f.t = mk(0.f, 0.f);
         }
     }
     const double tol2 = a.tol * a.tol;
@@ -848,26 +869,27 @@ __device__ __forceinline__ void refine_tile(const MixedArgs &a, const float2 *bu
             // and never accept a pair.  With an FP32 Jacobian each Newton step
             // gains a factor of about eps32 * cond, so most pairs reach the
             // acceptance level after the second correction: with ff_steps = 2
-            // the one FP64 residual is usually the accepting one.  Step 0: v0 and
-            // lambda0 are FP32 numbers (dx holds v0); step 1: v and lambda split
-            // into FP32 heads (into dx, free until the next correction) and tails.
+            // the one FP64 residual is usually the accepting one.  v is held in
+            // float-float meanwhile (the corrections are added on the FP32
+            // pipe); lambda is split into an FP32 head and tail.
             if (step == 0) {
-                ff_residual<MAXN, false>(n, Ah, Al, dx, vl, T.ld(k, k), mk(0.f, 0.f), r32);
+                ff_residual<MAXN, false>(n, Ah, Al, v, T.ld(k, k), mk(0.f, 0.f), r32);
             } else {
-                for (int i = 0; i < n; ++i) {
-                    dx[i] = down(v[i]);
-                    vl[i] = down(csub(v[i], up(dx[i])));
-                }
                 const cx<float> lh = down(lam);
-                ff_residual<MAXN, true>(n, Ah, Al, dx, vl, lh, down(csub(lam, up(lh))), r32);
+                ff_residual<MAXN, true>(n, Ah, Al, v, lh, down(csub(lam, up(lh))), r32);
             }
         } else {
-            // FP64 residual: the one that accepts
+            // FP64 residual: the one that accepts.  The first one turns v into FP64.
+            if (step == ff_steps)
+                for (int i = 0; i < n; ++i) {
+                    const cx<float> h = v[i].f.h, t = v[i].f.t;
+                    v[i].d = cadd(up(h), up(t));
+                }
             double rn2 = 0.0, vn2 = 0.0;
             for (int i = 1; i <= n; ++i) {
-                const cx<double> vi = v[i - 1];
+                const cx<double> vi = v[i - 1].d;
                 cx<double> acc = mk(-(lam.r * vi.r - lam.i * vi.i), -(lam.r * vi.i + lam.i * vi.r));
-                for (int j = 1; j <= n; ++j) acc = cmac(acc, A.ld(i, j), v[j - 1]);
+                for (int j = 1; j <= n; ++j) acc = cmac(acc, A.ld(i, j), v[j - 1].d);
                 rn2 = fma(acc.i, acc.i, fma(acc.r, acc.r, rn2));
                 vn2 = fma(vi.i, vi.i, fma(vi.r, vi.r, vn2));
                 r32[i - 1] = down(acc);
@@ -908,7 +930,12 @@ __device__ __forceinline__ void refine_tile(const MixedArgs &a, const float2 *bu
         for (int i = 1; i <= n; ++i) {
             cx<float> s = mk(0.f, 0.f);
             for (int j = 1; j <= n; ++j) s = cmac(s, Z.ld(i, j), dx[j - 1]);
-            v[i - 1] = cadd(v[i - 1], up(s));
+            if (step < ff_steps) {
+                ff_add(v[i - 1].f.h.r, v[i - 1].f.t.r, s.r);
+                ff_add(v[i - 1].f.h.i, v[i - 1].f.t.i, s.i);
+            } else {
+                v[i - 1].d = cadd(v[i - 1].d, up(s));
+            }
         }
         lam = cadd(lam, up(dl));
     }
@@ -929,18 +956,19 @@ __device__ __forceinline__ void refine_tile(const MixedArgs &a, const float2 *bu
     const long long vo = soa_off_m(m, n, tc);
     const VecSoA<double> E{a.rE + vo, a.iE + vo, tc};
     E.st(k, lam);
+    // (accepted pairs passed an FP64 residual, so v is in its FP64 form)
     double scale = 1.0;
     if (a.vnorm == 1) {
         double mx = 0.0;
-        for (int i = 0; i < n; ++i) mx = fmax(mx, cabs1(v[i]));
+        for (int i = 0; i < n; ++i) mx = fmax(mx, cabs1(v[i].d));
         scale = mx > 0.0 ? 1.0 / mx : 1.0;
     } else if (a.vnorm == 2) {
         double s2 = 0.0;
-        for (int i = 0; i < n; ++i) s2 = fma(v[i].i, v[i].i, fma(v[i].r, v[i].r, s2));
+        for (int i = 0; i < n; ++i) s2 = fma(v[i].d.i, v[i].d.i, fma(v[i].d.r, v[i].d.r, s2));
         scale = s2 > 0.0 ? 1.0 / sqrt(s2) : 1.0;
     }
     const MatSoA<double> Vo{a.rV + mo, a.iV + mo, tc, n};
-    for (int i = 1; i <= n; ++i) Vo.st(i, k, cscal(v[i - 1], scale));
+    for (int i = 1; i <= n; ++i) Vo.st(i, k, cscal(v[i - 1].d, scale));
 }
 
 // Tiles of kRefineThreads pairs, block-strided: the grid is either one block
