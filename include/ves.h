@@ -177,7 +177,7 @@ size_t ves_eigensolve_workspace_size(int dim, int block_cnt, int thread_cnt, con
  * shared by every call on the device, so calls that can run at the same time
  * on different streams must each pass their own workspace), otherwise it must
  * hold ves_eigensolve_workspace_size() bytes, 256-byte aligned.  Asynchronous
- * on `stream`; for large batches of dim > 16 the FP32 + refinement form runs
+ * on `stream`; for large batches of dim >= 32 the FP32 + refinement form runs
  * on two library streams forked from `stream` by an event and joined back into
  * it (VES_MIXED_OVERLAP=0 / 1 in the environment forces this off / on).
  * The two library streams are shared by all callers on a device: concurrent

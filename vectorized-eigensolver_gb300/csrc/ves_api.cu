@@ -757,11 +757,13 @@ int ves_eigensolve(int dim, int block_cnt, int thread_cnt, const double *rA, con
     // stream.  So does a call whose stream is being captured: the library streams
     // are shared by every caller on the device, and forking them into one
     // caller's capture would pull other callers' work into that graph.
-    // Overlap pays for n > 16; for n <= 16 the stages measured faster one after
-    // the other (n=8: 47.9 against 44.8 M/s, n=16 with the group Schur kernel:
-    // 7.04 against 5.17 M/s on GB300).  VES_MIXED_OVERLAP=1 / 0 forces it on / off.
+    // Overlap pays for n >= 32; below, the stages measured faster one after the
+    // other on GB300 (FP32+refine eigensolves/s, serial against overlapped: n=8
+    // 47.9 / 44.8 M/s, n=16 (group Schur kernel) 7.04 / 5.17, n=20 (warp Schur
+    // kernel) 3.78 / 3.05, n=24 2.42 / 2.23, n=28 1.60 / 1.48; n=32 1.095 / 1.106).
+    // VES_MIXED_OVERLAP=1 / 0 forces it on / off.
     const char *ov = getenv("VES_MIXED_OVERLAP");
-    const bool overlap = ov && (ov[0] == '0' || ov[0] == '1') ? ov[0] == '1' : dim > 16;
+    const bool overlap = ov && (ov[0] == '0' || ov[0] == '1') ? ov[0] == '1' : dim >= 32;
     cudaStream_t s_schur = nullptr, s_refine = nullptr;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     if (!cuda_ok(cudaStreamIsCapturing(st, &cap), "cudaStreamIsCapturing")) return VES_ERR_CUDA;

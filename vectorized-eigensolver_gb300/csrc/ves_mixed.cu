@@ -1089,7 +1089,14 @@ namespace {
 // 21.0, n=12 14.1 -> 9.3, n=16 5.84 -> 4.75 M/s (its Schur stage alone at
 // n=16: 90 ms per 1,048,576 matrices against about 78 for the lane kernel,
 // and it leaves less of each SM to the refinement running beside it).
-// Default: G = 32 for 24 <= n <= 32, the lane kernel otherwise.
+// Default: G = 32 for 24 <= n <= 32, the lane kernel otherwise.  Later, with
+// the warp kernel's two synchronisations per step and the float-float
+// refinement, stages one after the other: n=17 lane 4.88 (5.30 overlapped),
+// warp 5.38 M/s; n=20 lane 3.03 (3.36), warp 3.78 M/s.  The group kernel
+// generalised to n <= 32 (a matrix per 8 or 16 lanes) measured slower than
+// the warp kernel at n = 17..32 (n=20 3.64 / 3.73, n=24 1.77 / 2.16, n=32
+// 0.58 / 0.95 M/s against 3.78, 2.42, 1.10).  Default now: G = 32 for
+// 17 <= n <= 32.
 // VES_MIXED_SCHUR overrides (tests and tuning): lane; warp (G = 16 for
 // n <= 16, G = 32 for n <= 32); warp16; warp32.
 int schur_group(int n)
@@ -1103,7 +1110,7 @@ int schur_group(int n)
     if (e && !strcmp(e, "group8")) return n <= 16 ? 8 : 0;
     if (n >= 11 && n <= 14) return 4;
     if (n >= 15 && n <= 16) return 8;
-    return (n >= 24 && n <= 32) ? 32 : 0;
+    return (n >= 17 && n <= 32) ? 32 : 0;
 }
 
 template <int G>
