@@ -394,7 +394,8 @@ def eig_distance(E1, E0, A, chunk=1 << 17):
 #   net     ves_shiftnet_config fields (robust Chamfer loss, delta 0.01)
 #   epochs  over the 200,000 training solutions
 #   polish  Aberth steps on all predictions of a matrix (FP32, on the Hessenberg
-#           form; more steps changed nothing on any order)
+#           form; more steps changed nothing on any order), then one FP64 Newton
+#           step per prediction inside the solve
 #   gate    predictions only while |H(I,I-1)| > gate * ||A||_F / sqrt(n); 0 = always
 LEARNED = {
     16: dict(net=dict(hidden=256, layers=4, fourier=8, loss=1, delta=0.01), epochs=150, polish=16, gate=0.0),
@@ -410,7 +411,8 @@ def measure_learned(n, N, train_count, steps, tc=512):
     + p3 A3 (order n): the network is trained (tcgen05 BF16 MLP) on
     `train_count` plain-solver solutions (param seed 5), then on a fresh batch
     (param seed 6) one step = network inference + the shift-seeded FP64 solve
-    (predictions polished by Aberth steps), against the plain FP64 solve
+    (predictions polished by Aberth steps in FP32 and one Newton step in FP64),
+    against the plain FP64 solve
     of the same batch."""
     import torch
     import ves
@@ -477,7 +479,8 @@ def measure_learned(n, N, train_count, steps, tc=512):
     polish_steps = int(wc[ves.VES_WORK_POLISH])
     h, L, F = cfg["net"]["hidden"], cfg["net"]["layers"], cfg["net"]["fourier"]
     kin = 3 + 2 * 3 * F + 2 * n
-    f64 = fp64_flops(n, float(sw.double().sum()), N)
+    # + the FP64 Newton step on each prediction (x and x' of Hyman's recurrence: 8 n^2)
+    f64 = fp64_flops(n, float(sw.double().sum()), N) + (N * 8.0 * n ** 3 if cfg["polish"] > 0 else 0.0)
     f32 = polish_steps * (8.0 * n * n + 10.0 * n) + (N * 40.0 / 3.0 * n ** 3 if n <= 32 else 0.0) + N * 2.0 * h * 2 * n
     fbf16 = N * 2.0 * (kin * h + (L - 1) * h * h)
     rl = roofline(ms_learned * 1e-3, fp64=f64, fp32=f32, bf16=fbf16, hbm=hbm_bytes(n, N))

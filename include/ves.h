@@ -134,10 +134,11 @@ typedef struct ves_options {
                         * is the better estimate); set it to the predictor's typical error; default 0 */
     int shift_polish;  /* ves_eigensolve_shifts: steps (0..64) of simultaneous Aberth iteration on det(H - sI)
                         * (FP32, Hyman's recurrence on the Hessenberg matrix) that refine all predictions of a
-                        * matrix together before the QR; a prediction that does not converge or lands on an
-                        * eigenvalue already seeded is dropped; for dim <= 32 this runs as a warp-per-matrix
-                        * pre-pass (environment VES_POLISH_METHOD=newton: each prediction on its own);
-                        * 0 (default) = none */
+                        * matrix together before the QR, then one FP64 Newton step per prediction on the
+                        * solve's own Hessenberg matrix; a prediction that does not converge or lands on an
+                        * eigenvalue already seeded is dropped; for dim <= 32 the FP32 steps run as a
+                        * warp-per-matrix pre-pass (environment VES_POLISH_METHOD=newton: each prediction on
+                        * its own; VES_POLISH_FP64_STEP=0: no FP64 step); 0 (default) = none */
     unsigned long long *work_counts; /* nullable DEVICE array of VES_WORK_COUNTS counters that the call ADDS to
                         * (zero them first; stream-ordered like the outputs): the work of the data-dependent
                         * stages, for flop accounting.  Default NULL. */

@@ -854,6 +854,64 @@ __device__ void polish_shifts_lane(const int n, const MatIlv<float> &Hf, const V
     }
 }
 
+// One Newton step in FP64 on det(H - s I) for every finite prediction in S,
+// H the solve's own FP64 Hessenberg matrix (real subdiagonal, as zgehrd
+// leaves it).  The FP32 polish works on an FP32 Hessenberg form of A, whose
+// eigenvalues are those of A to about 1e-6 of their scale; from there one
+// FP64 step (Hyman's recurrence and its derivative, as in polish_shifts_lane)
+// takes a prediction to about 1e-12, and a QR sweep with that shift all but
+// deflates its eigenvalue.  x and x' live in X and DX (n entries each).  A
+// step that is non-finite or longer than `maxstep` (the FP32 polish had not
+// converged there) leaves the prediction as it was; a zero subdiagonal (H
+// already splits) leaves all of them.
+template <class MH>
+__device__ void newton64_shifts_lane(const int n, const MH &H, const VecIlv<double> &S, const VecIlv<double> &X,
+                                     const VecIlv<double> &DX, const double maxstep)
+{
+    for (int i = 2; i <= n; ++i)
+        if (H.ld(i, i - 1).r == 0.0) return;
+    for (int k = 1; k <= n; ++k) {
+        const cx<double> s = S.ld(k);
+        if (nonfinite(s.r) || nonfinite(s.i)) continue;
+        X.st(n, mk(1.0, 0.0));
+        DX.st(n, mk(0.0, 0.0));
+        for (int i = n; i >= 2; --i) {
+            const cx<double> d = csub(H.ld(i, i), s);
+            const cx<double> xi = X.ld(i);
+            cx<double> acc = cmul(d, xi);
+            cx<double> dacc = csub(cmul(d, DX.ld(i)), xi);
+            for (int j = i + 1; j <= n; ++j) {
+                const cx<double> h = H.ld(i, j);
+                acc = cmac(acc, h, X.ld(j));
+                dacc = cmac(dacc, h, DX.ld(j));
+            }
+            const double rs = -1.0 / H.ld(i, i - 1).r;
+            cx<double> xn = cscal(acc, rs), dxn = cscal(dacc, rs);
+            if (cabs1(xn) > 1e150) {  // rescale x, x' together (the Newton ratio is scale free)
+                for (int j = i; j <= n; ++j) {
+                    X.st(j, cscal(X.ld(j), 1e-150));
+                    DX.st(j, cscal(DX.ld(j), 1e-150));
+                }
+                xn = cscal(xn, 1e-150);
+                dxn = cscal(dxn, 1e-150);
+            }
+            X.st(i - 1, xn);
+            DX.st(i - 1, dxn);
+        }
+        const cx<double> d1 = csub(H.ld(1, 1), s);
+        const cx<double> x1 = X.ld(1);
+        cx<double> r = cmul(d1, x1);
+        cx<double> rp = csub(cmul(d1, DX.ld(1)), x1);
+        for (int j = 2; j <= n; ++j) {
+            const cx<double> h = H.ld(1, j);
+            r = cmac(r, h, X.ld(j));
+            rp = cmac(rp, h, DX.ld(j));
+        }
+        const cx<double> delta = cdiv(r, rp);
+        if (!nonfinite(delta.r) && !nonfinite(delta.i) && cabs1(delta) <= maxstep) S.st(k, csub(s, delta));
+    }
+}
+
 // kDefl64 (FP32 data only): the deflation test in FP64 (deflation_scan64).
 template <class R, bool kSchur = true, bool kDefl64 = false, class MH, class MZ, class SP = NoShiftPredictions>
 __device__ void zlahqr_warp(const int n, const MH &H, const MZ &Z, const bool valid, const int max_its,

@@ -146,6 +146,11 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
                         polish_shifts_lane<64>(n, Hf, S, a.shift_polish, tol, keep, dup);
                 }
             }
+            if (a.shift_newton64 && valid && !(status & ST_NONFINITE) && n >= 2) {
+                // x in the work vector, x' where the FP32 copy of H was (n <= (n^2 + 1) / 2 entries)
+                const VecIlv<double> DX{base + (2LL * n * n + n) * 32};
+                newton64_shifts_lane(n, H, S, W, DX, 1e-4 * scale);
+            }
             sp.S = S;
             sp.n = n;
             sp.sweeps = a.shift_sweeps;
