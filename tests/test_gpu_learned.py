@@ -176,3 +176,35 @@ def test_polish_separates_duplicate_predictions(n):
     assert sweeps["aberth"] < 0.8 * plain
     if "newton" in sweeps:
         assert sweeps["aberth"] < 0.95 * sweeps["newton"]
+
+
+@pytest.mark.parametrize("n", [16, 40])
+def test_fp64_newton_step_cuts_sweeps(n):
+    """After the FP32 polish (predictions at ~1e-6 of the eigenvalue scale), one
+    FP64 Newton step on the solve's own Hessenberg matrix brings them to ~1e-12:
+    fewer QR sweeps than without it (VES_POLISH_FP64_STEP=0), the same bar."""
+    import torch
+    N = 4096
+    p, rA, iA = learned_shift.family(N, n, param_seed=16)
+    rE0, iE0, sw0 = learned_shift.solve_plain(n, N, rA, iA, TC)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    rS = rE0 + 1e-2 * torch.randn(rE0.shape, generator=g, device="cuda", dtype=torch.float64)
+    iS = iE0 + 1e-2 * torch.randn(rE0.shape, generator=g, device="cuda", dtype=torch.float64)
+    E0 = ves.complex_vec_from_soa(rE0.cpu().numpy(), iE0.cpu().numpy(), n, TC)
+    nA = np.linalg.norm(ves.complex_from_soa(rA.cpu().numpy(), iA.cpu().numpy(), n, TC), axis=(1, 2))
+    sweeps = {}
+    for step in ("1", "0"):
+        os.environ["VES_POLISH_FP64_STEP"] = step
+        try:
+            rE, iE, st, sw, fb, res = solve_shifts(n, N, rA, iA, rS, iS, shift_polish=8)
+        finally:
+            del os.environ["VES_POLISH_FP64_STEP"]
+        assert res <= 1e-13
+        E = ves.complex_vec_from_soa(rE.cpu().numpy(), iE.cpu().numpy(), n, TC)
+        _, err, _ = match_eigs(E, E0)
+        assert (err / nA).max() <= 1e-12
+        assert ((st & ~ves.VES_STATUS_SHIFT_FALLBACK) == 0).all()
+        sweeps[step] = sw.double().mean().item()
+    print("sweeps per matrix: plain %.2f, with / without the FP64 step %.2f / %.2f"
+          % (sw0.double().mean().item(), sweeps["1"], sweeps["0"]))
+    assert sweeps["1"] < 0.95 * sweeps["0"]
