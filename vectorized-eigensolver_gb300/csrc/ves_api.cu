@@ -248,9 +248,17 @@ bool do_eigensolver(int dim, int bc, int tc, double *rA, double *iA, double *rE,
     double *dEr = b.d(4, nv), *dEi = b.d(5, nv);
     NEED(dAr); NEED(dAi); NEED(dVr); NEED(dVi); NEED(dEr); NEED(dEi);
 
-    constexpr long long kMinChunk = 65536;  // matrices per chunk: keeps each launch's persistent grid busy
-    constexpr long long kMaxChunks = 8;
-    long long nchunks = std::min<long long>(kMaxChunks, std::max<long long>(1, g.N / kMinChunk));
+    // Up to 16 chunks of at least 65,536 matrices (each launch's persistent grid
+    // stays busy).  1,048,576 x 16x16 from pinned host buffers on GB300, chunks
+    // -> ms per call: 8 -> 638, 12 -> 632, 16 -> 625, 24 -> 671, 32 -> 715 (the
+    // device-resident solve: 621): the first copy-in and the last copy-out are
+    // what is not hidden, and more, smaller launches leave more tails.
+    constexpr long long kMinChunk = 65536;
+    long long nchunks = std::min<long long>(16, std::max<long long>(1, g.N / kMinChunk));
+    if (const char *e = getenv("VES_DROPIN_CHUNKS")) {  // tuning: the chunk count itself
+        const int v = atoi(e);
+        if (v >= 1 && v <= 64) nchunks = v;
+    }
     nchunks = std::min<long long>(nchunks, bc);
     const long long cb = (bc + nchunks - 1) / nchunks;  // blocks per chunk
     nchunks = (bc + cb - 1) / cb;
