@@ -384,12 +384,16 @@ def test_device_stage_entry_points():
     np.testing.assert_array_equal(dr.cpu().numpy(), hr)
 
 
-def test_dropin_pipeline_chunks_equal_one_launch():
+@pytest.mark.parametrize("chunks", [None, "7"])
+def test_dropin_pipeline_chunks_equal_one_launch(chunks, monkeypatch):
     """The drop-in eigensolver() splits a large batch into chunks of SoA blocks
     solved on two streams; its results equal one device launch bit for bit
-    (unequal chunks: 3 chunks of 141, 141 and 139 blocks)."""
+    (unequal chunks: by default 3 chunks of 141, 141 and 139 blocks; with
+    VES_DROPIN_CHUNKS=7, six of 61 and one of 55)."""
     import torch
     import workloads
+    if chunks:
+        monkeypatch.setenv("VES_DROPIN_CHUNKS", chunks)
     n, tc, bc = 4, 512, 421
     N = bc * tc
     rA, iA = workloads.gaussian_soa(N, n, seed=11, thread_cnt=tc)
