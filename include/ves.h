@@ -138,7 +138,7 @@ typedef struct ves_options {
                         * solve's own Hessenberg matrix; a prediction that does not converge or lands on an
                         * eigenvalue already seeded is dropped; for dim <= 32 the FP32 steps run as a
                         * warp-per-matrix pre-pass (environment VES_POLISH_METHOD=newton: each prediction on
-                        * its own; VES_POLISH_FP64_STEP=0: no FP64 step); 0 (default) = none */
+                        * its own; VES_POLISH_FP64_STEP=0 / 2: no / two FP64 steps); 0 (default) = none */
     unsigned long long *work_counts; /* nullable DEVICE array of VES_WORK_COUNTS counters that the call ADDS to
                         * (zero them first; stream-ordered like the outputs): the work of the data-dependent
                         * stages, for flop accounting.  Default NULL. */

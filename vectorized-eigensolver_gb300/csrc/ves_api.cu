@@ -930,9 +930,9 @@ int ves_eigensolve_shifts(int dim, int block_cnt, int thread_cnt, const double *
     a.shift_gate = o.shift_gate;
     a.shift_polish = o.shift_polish;
     // with the polish, one FP64 Newton step per prediction on the solve's own
-    // Hessenberg matrix; VES_POLISH_FP64_STEP=0 leaves it out (tuning)
+    // Hessenberg matrix; VES_POLISH_FP64_STEP=0 / 2 takes none / two (tuning)
     const char *f64s = getenv("VES_POLISH_FP64_STEP");
-    a.shift_newton64 = (o.shift_polish > 0 && !(f64s && f64s[0] == '0')) ? 1 : 0;
+    a.shift_newton64 = o.shift_polish > 0 ? ((f64s && (f64s[0] == '0' || f64s[0] == '2')) ? f64s[0] - '0' : 1) : 0;
     a.fallbacks = fallbacks;
     a.blocks_per_sm = o.blocks_per_sm;
     cudaStream_t st = (cudaStream_t)stream;

@@ -52,7 +52,7 @@ struct FusedArgs {
     int shift_sweeps;
     float shift_gate;  // predictions used only while |H(I,I-1)| > shift_gate * ||A||_F / sqrt(n)
     int shift_polish;  // Aberth steps on det(H - sI) per prediction (FP32) before the QR; 0 = none
-    int shift_newton64;  // 1: then one FP64 Newton step per prediction on the solve's own H
+    int shift_newton64;  // then this many FP64 Newton steps per prediction on the solve's own H
     int *fallbacks;
     int blocks_per_sm;  // persistent grid: blocks (4 warps) per SM; 0 = default
 };

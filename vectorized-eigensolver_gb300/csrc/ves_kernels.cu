@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
             if (a.shift_newton64 && valid && !(status & ST_NONFINITE) && n >= 2) {
                 // x in the work vector, x' where the FP32 copy of H was (n <= (n^2 + 1) / 2 entries)
                 const VecIlv<double> DX{base + (2LL * n * n + n) * 32};
-                newton64_shifts_lane(n, H, S, W, DX, 1e-4 * scale);
+                for (int st = 0; st < a.shift_newton64; ++st) newton64_shifts_lane(n, H, S, W, DX, 1e-4 * scale);
             }
             sp.S = S;
             sp.n = n;
