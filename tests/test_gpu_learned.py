@@ -208,3 +208,48 @@ def test_fp64_newton_step_cuts_sweeps(n):
     print("sweeps per matrix: plain %.2f, with / without the FP64 step %.2f / %.2f"
           % (sw0.double().mean().item(), sweeps["1"], sweeps["0"]))
     assert sweeps["1"] < 0.95 * sweeps["0"]
+
+
+@pytest.mark.parametrize("n", [8, 16, 40])
+def test_polish_special_matrices(n):
+    """The Aberth polish and the FP64 Newton step on structured inputs: an
+    upper-triangular matrix (the Hessenberg form splits at once: no FP64 step),
+    a diagonal one, a repeated eigenvalue (2 I plus a rank-one term), the zero
+    matrix, and predictions that are NaN or infinite.  Every solve meets the
+    plain solver's bar against LAPACK."""
+    import torch
+    rng = np.random.default_rng(900 + n)
+    N = TC
+    A = rng.standard_normal((N, n, n)) + 1j * rng.standard_normal((N, n, n))
+    A[1] = np.triu(A[1])
+    A[2] = np.diag(np.arange(1, n + 1) * (1 + 0.5j))
+    u = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    A[3] = 2 * np.eye(n) + np.outer(u, u.conj()) / n
+    A[4] = 0
+    E = np.linalg.eigvals(A)
+    P = E + 1e-2 * (rng.standard_normal(E.shape) + 1j * rng.standard_normal(E.shape))
+    P[5, :] = np.nan
+    P[6, 0] = np.inf
+    rA, iA = (torch.from_numpy(x).cuda() for x in ves.soa_from_complex(A, TC))
+    rS, iS = (torch.from_numpy(x).cuda() for x in ves.soa_vec_from_complex(P, TC))
+    rE, iE, st, sw, fb, res = solve_shifts(n, N, rA, iA, rS, iS, shift_polish=8)
+    Eg = ves.complex_vec_from_soa(rE.cpu().numpy(), iE.cpu().numpy(), n, TC)
+    V = ves.complex_from_soa(*(t.cpu().numpy() for t in solve_vectors(n, N, rA, iA, rS, iS)), n, TC)
+    nA = np.maximum(np.linalg.norm(A, axis=(1, 2)), 1.0)
+    _, err, _ = match_eigs(Eg, E)
+    assert (err / nA).max() <= 1e-12
+    r = np.linalg.norm(A @ V - V * Eg[:, None, :], axis=1) / (nA[:, None] * np.maximum(np.linalg.norm(V, axis=1), 1e-300))
+    assert r.max() <= 1e-13
+    assert ((st & ~ves.VES_STATUS_SHIFT_FALLBACK) == 0).all()
+
+
+def solve_vectors(n, N, rA, iA, rS, iS):
+    """The eigenvectors of the shift-seeded solve with shift_polish=8 (planes)."""
+    import torch
+    rE = torch.empty(N * n, dtype=torch.float64, device="cuda")
+    iE = torch.empty_like(rE)
+    rV, iV = torch.empty_like(rA), torch.empty_like(iA)
+    ves.eigensolve_shifts(n, N // TC, TC, rA, iA, rE, iE, rV, iV, rS, iS,
+                          options=ves.default_options(shift_polish=8))
+    torch.cuda.synchronize()
+    return rV, iV
