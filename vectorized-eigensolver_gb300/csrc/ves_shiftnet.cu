@@ -61,6 +61,87 @@ cudaError_t launch_persistent(int M, int N, int K, const __nv_bfloat16 *a, int l
     return cudaGetLastError();
 }
 
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+// (no link-time dependency on libcuda).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled()
+{
+    static EncodeTiledFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// Tensor map of a row-major rows x K BF16 matrix (leading dimension ld) read
+// in boxes of 8 elements (16 bytes) x box_rows; false if the driver rejects it
+// (base not 16-byte aligned, ld * 2 not a multiple of 16, ...).
+bool bf16_box_map(CUtensorMap *map, const void *base, int rows, int K, int ld, int box_rows)
+{
+    const EncodeTiledFn fn = encode_tiled();
+    if (!fn || ((uintptr_t)base & 15) != 0 || (ld % 8) != 0 || K < 8 || rows < 1 || box_rows > 256) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {8, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The persistent GEMM with TMA operand loads; cudaErrorNotSupported when a
+// tensor map cannot be made for these operands (the caller then uses cp.async).
+template <int NT>
+cudaError_t launch_persistent_tma(int M, int N, int K, const __nv_bfloat16 *a, int lda, const __nv_bfloat16 *b,
+                                  int ldb, const float *bias, int act, __nv_bfloat16 *c, float *cf, int ldc, int *err,
+                                  cudaStream_t st)
+{
+    CUtensorMap ta, tb;
+    if (!bf16_box_map(&ta, a, M, K, lda, tc::kM) || !bf16_box_map(&tb, b, N, K, ldb, NT)) return cudaErrorNotSupported;
+    const int smem = (tc::kM + NT) * K * 2;
+    cudaError_t e = cudaFuncSetAttribute(tc::gemm_bf16_tma_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (tc::kM + NT) * 256 * 2);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    constexpr int kCols = NT <= 32 ? 32 : (NT <= 64 ? 64 : (NT <= 128 ? 128 : 256));
+    const int per_sm = std::max(1, std::min(512 / kCols, (220 * 1024) / smem));
+    const int mtiles = (M + tc::kM - 1) / tc::kM;
+    const unsigned gx = (unsigned)std::max(1, std::min(mtiles, std::max(sms, 1) * per_sm));
+    tc::gemm_bf16_tma_kernel<NT><<<dim3(gx, (N + NT - 1) / NT), 128, smem, st>>>(ta, tb, M, N, K, bias, act, c, cf,
+                                                                               ldc, err);
+    return cudaGetLastError();
+}
+
+// The persistent GEMM: TMA operand loads for more than 16 row tiles, cp.async
+// for fewer (a training batch) or where no tensor map can be made.  GB300,
+// 256 x 256 weights, GELU: M = 1,048,576 0.835 ms with TMA against 1.043 ms
+// (165 against 132 TFLOP/s), M = 262,144 0.226 against 0.282 ms; M = 1,024
+// about the same either way.  VES_GEMM_TMA=1 / 0 forces TMA / cp.async.
+template <int NT>
+cudaError_t launch_persistent_any(int M, int N, int K, const __nv_bfloat16 *a, int lda, const __nv_bfloat16 *b,
+                                  int ldb, const float *bias, int act, __nv_bfloat16 *c, float *cf, int ldc, int *err,
+                                  cudaStream_t st)
+{
+    const char *e = getenv("VES_GEMM_TMA");
+    const bool tma = e && (e[0] == '0' || e[0] == '1') ? e[0] == '1' : (M + tc::kM - 1) / tc::kM > 16;
+    if (tma) {
+        const cudaError_t r = launch_persistent_tma<NT>(M, N, K, a, lda, b, ldb, bias, act, c, cf, ldc, err, st);
+        if (r != cudaErrorNotSupported) return r;
+    }
+    return launch_persistent<NT>(M, N, K, a, lda, b, ldb, bias, act, c, cf, ldc, err, st);
+}
+
 }  // namespace
 
 // The persistent kernel when K <= 256 and the shapes allow 16-byte vector
@@ -77,10 +158,10 @@ cudaError_t launch_gemm_bf16(int M, int N, int K, const void *A, int lda, const 
         // few row tiles (a training batch): narrower column tiles give more CTAs
         // (M = 1,024, N = 256: 32 instead of 8)
         if ((M + tc::kM - 1) / tc::kM <= 16 && N > 64 && N % 64 == 0)
-            return launch_persistent<64>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
-        if (N > 128) return launch_persistent<256>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
-        if (N > 64) return launch_persistent<128>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
-        return launch_persistent<64>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
+            return launch_persistent_any<64>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
+        if (N > 128) return launch_persistent_any<256>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
+        if (N > 64) return launch_persistent_any<128>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
+        return launch_persistent_any<64>(M, N, K, a, lda, b, ldb, bias, act, c, Cf, ldc, err, st);
     }
     const unsigned gx = (unsigned)((M + tc::kM - 1) / tc::kM);
     if (N > 64) {
@@ -529,6 +610,9 @@ void load_shiftnet_kernels()
     load_kernel(tc::gemm_bf16_persistent_kernel<64>);
     load_kernel(tc::gemm_bf16_persistent_kernel<128>);
     load_kernel(tc::gemm_bf16_persistent_kernel<256>);
+    load_kernel(tc::gemm_bf16_tma_kernel<64>);
+    load_kernel(tc::gemm_bf16_tma_kernel<128>);
+    load_kernel(tc::gemm_bf16_tma_kernel<256>);
     load_kernel(tc::gemm_bf16_kernel<64>);
     load_kernel(tc::gemm_bf16_kernel<256>);
     load_kernel(features_kernel);

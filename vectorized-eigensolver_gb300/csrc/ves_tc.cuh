@@ -19,6 +19,7 @@
 // error, stops issuing work, and still releases its TMEM columns.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (the TMA tensor-map type)
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -359,6 +360,154 @@ __global__ void __launch_bounds__(128) gemm_bf16_persistent_kernel(const __nv_bf
         if (tid == 0) (void)mbar_wait(&bar, phase ^ 1);
         if (tid == 0 && err) atomicExch(err, 1);
         cp_async_wait_all();
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols));
+}
+
+// ---------------------------------------------------------------------------
+// The persistent GEMM with its operands loaded by the Tensor Memory Accelerator
+// (cp.async.bulk.tensor): one thread issues, per 16-byte column of K, a 2-D box
+// of 8 elements x 128 rows of A (x NT rows of B) from a tensor map.  A box
+// lands row after row, 16 bytes a row, so each box is a column of core
+// matrices: M-adjacent core matrices 128 bytes apart (stride-dimension offset)
+// and K-adjacent ones a box apart (leading-dimension offset 128 x 16 bytes for
+// A, NT x 16 for B).  Rows past M or N are filled with zeros by the TMA unit.
+// The x coordinate of every box is a multiple of 8 elements (16 bytes).  The
+// boxes of a tile arrive on one mbarrier with the tile's byte count; the next
+// A-tile is fetched while the epilogue drains TMEM.  Every wait is bounded; on
+// a timeout the kernel waits (bounded) for its own copies and MMAs still in
+// flight, records the error and frees its TMEM.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
+template <int NT>
+__global__ void __launch_bounds__(128) gemm_bf16_tma_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                            const __grid_constant__ CUtensorMap tmB, int M, int N,
+                                                            int K, const float *bias, int act, __nv_bfloat16 *C,
+                                                            float *Cf, int ldc, int *err)
+{
+    static_assert(NT % 16 == 0 && NT >= 16 && NT <= 256, "N tile");
+    constexpr int kCols = NT <= 32 ? 32 : (NT <= 64 ? 64 : (NT <= 128 ? 128 : 256));
+    extern __shared__ __align__(1024) unsigned char dsm[];
+    unsigned char *sA = dsm;
+    unsigned char *sB = dsm + (size_t)kM * K * 2;
+    __shared__ __align__(8) uint64_t bar;   // MMAs of a tile done
+    __shared__ __align__(8) uint64_t tbar;  // a tile's TMA boxes landed
+    __shared__ uint32_t tmem_base;
+    __shared__ int failed;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int n0 = blockIdx.y * NT;
+    const int mtiles = (M + kM - 1) / kM;
+    const int kcs = K / 8;  // 16-byte columns of K: one box each
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
+                     "r"(kCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        mbar_init(&tbar, 1);
+        failed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    int tile = blockIdx.x;
+    if (tid == 0 && tile < mtiles) {  // B (this CTA's N-tile, all of K) and the first A-tile
+        mbar_expect_tx(&tbar, (uint32_t)((kM + NT) * K * 2));
+        for (int kc = 0; kc < kcs; ++kc) tma_load_2d(smem_addr(sB) + kc * NT * 16, &tmB, kc * 8, n0, &tbar);
+        for (int kc = 0; kc < kcs; ++kc) tma_load_2d(smem_addr(sA) + kc * kM * 16, &tmA, kc * 8, tile * kM, &tbar);
+    }
+    const uint32_t tmem = tmem_base;
+    constexpr uint32_t idesc = make_idesc(kM, NT);
+
+    unsigned phase = 0, tphase = 0;
+    for (; tile < mtiles; tile += gridDim.x) {
+        if (tid == 0) {
+            if (!mbar_wait(&tbar, tphase)) {
+                failed = 1;
+                mbar_arrive(&bar);  // release the other threads' wait below
+            } else {
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                for (int s = 0; s < K / 16; ++s) {
+                    const uint64_t da = make_desc(smem_addr(sA) + s * 2 * kM * 16, kM * 16, 128);
+                    const uint64_t db = make_desc(smem_addr(sB) + s * 2 * NT * 16, NT * 16, 128);
+                    mma_bf16(tmem, da, db, idesc, s > 0 ? 1u : 0u);
+                }
+                mma_commit(&bar);
+            }
+            tphase ^= 1;
+        }
+        const bool ok = mbar_wait(&bar, phase);
+        phase ^= 1;
+        if (!ok) failed = 1;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        __syncthreads();  // every thread saw the MMAs complete (or the failure)
+        if (failed) break;
+        // the MMAs have read sA: fetch the next tile's A while draining TMEM
+        const int next = tile + gridDim.x;
+        if (tid == 0 && next < mtiles) {
+            mbar_expect_tx(&tbar, (uint32_t)(kM * K * 2));
+            for (int kc = 0; kc < kcs; ++kc)
+                tma_load_2d(smem_addr(sA) + kc * kM * 16, &tmA, kc * 8, next * kM, &tbar);
+        }
+        const int row = tile * kM + warp * 32 + lane;
+        for (int cb = 0; cb < NT; cb += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb, v);
+            const int col = n0 + cb;
+            if (row < M && col < N) {  // N is a multiple of 16: a chunk is all in or all out
+#pragma unroll
+                for (int i = 0; i < 16; ++i) v[i] += bias ? bias[col + i] : 0.f;
+                if (Cf) {
+                    float4 *dst = reinterpret_cast<float4 *>(Cf + (size_t)row * ldc + col);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                }
+                if (C) {
+                    uint32_t pk[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const float x0 = act == 1 ? gelu(v[2 * q]) : v[2 * q];
+                        const float x1 = act == 1 ? gelu(v[2 * q + 1]) : v[2 * q + 1];
+                        __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+                        pk[q] = *reinterpret_cast<uint32_t *>(&h);
+                    }
+                    uint4 *dst = reinterpret_cast<uint4 *>(C + (size_t)row * ldc + col);
+                    dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                    dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();  // TMEM drained before the next tile's MMAs
+    }
+    if (failed && tid == 0) {
+        // a wait gave up: one more bounded wait for the copies and MMAs still in
+        // flight (the phases that did not complete), then report
+        (void)mbar_wait(&tbar, tphase ^ 1);
+        (void)mbar_wait(&bar, phase ^ 1);
+        if (err) atomicExch(err, 1);
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
