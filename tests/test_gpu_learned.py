@@ -115,7 +115,7 @@ def test_polish_far_predictions_dropped(n):
     assert fb.sum().item() == 0
 
 
-@pytest.mark.parametrize("n", [16, 32, 40])
+@pytest.mark.parametrize("n", [16, 32, 40, 64])
 def test_polish_recovers_noisy_predictions(n):
     """Eigenvalues with 1% noise as predictions: the Newton polish brings them
     back to FP32 accuracy, the QR needs clearly fewer sweeps, the result meets
@@ -178,7 +178,7 @@ def test_polish_separates_duplicate_predictions(n):
         assert sweeps["aberth"] < 0.95 * sweeps["newton"]
 
 
-@pytest.mark.parametrize("n", [16, 40])
+@pytest.mark.parametrize("n", [16, 40, 64])
 def test_fp64_newton_step_cuts_sweeps(n):
     """After the FP32 polish (predictions at ~1e-6 of the eigenvalue scale), one
     FP64 Newton step on the solve's own Hessenberg matrix brings them to ~1e-12:
