@@ -479,9 +479,11 @@ def measure_learned(n, N, train_count, steps, tc=512):
     polish_steps = int(wc[ves.VES_WORK_POLISH])
     h, L, F = cfg["net"]["hidden"], cfg["net"]["layers"], cfg["net"]["fourier"]
     kin = 3 + 2 * 3 * F + 2 * n
-    # + the FP64 Newton step on each prediction (x and x' of Hyman's recurrence: 8 n^2)
-    f64 = fp64_flops(n, float(sw.double().sum()), N) + (N * 8.0 * n ** 3 if cfg["polish"] > 0 else 0.0)
-    f32 = polish_steps * (8.0 * n * n + 10.0 * n) + (N * 40.0 / 3.0 * n ** 3 if n <= 32 else 0.0) + N * 2.0 * h * 2 * n
+    # + the Newton step on each prediction: Hyman's recurrence for r in FP64 (4 n^2),
+    # for r' in FP32 (4 n^2, with the FP32 work below)
+    f64 = fp64_flops(n, float(sw.double().sum()), N) + (N * 4.0 * n ** 3 if cfg["polish"] > 0 else 0.0)
+    f32 = (polish_steps * (8.0 * n * n + 10.0 * n) + (N * 40.0 / 3.0 * n ** 3 if n <= 32 else 0.0) + N * 2.0 * h * 2 * n
+           + (N * 4.0 * n ** 3 if cfg["polish"] > 0 else 0.0))
     fbf16 = N * 2.0 * (kin * h + (L - 1) * h * h)
     rl = roofline(ms_learned * 1e-3, fp64=f64, fp32=f32, bf16=fbf16, hbm=hbm_bytes(n, N))
     passed = ver["max_residual"] <= RES_TOL and ver["nonfinite"] == 0 and err <= 1e-12 and other == 0

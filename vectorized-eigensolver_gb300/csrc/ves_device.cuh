@@ -858,56 +858,59 @@ __device__ void polish_shifts_lane(const int n, const MatIlv<float> &Hf, const V
 // H the solve's own FP64 Hessenberg matrix (real subdiagonal, as zgehrd
 // leaves it).  The FP32 polish works on an FP32 Hessenberg form of A, whose
 // eigenvalues are those of A to about 1e-6 of their scale; from there one
-// FP64 step (Hyman's recurrence and its derivative, as in polish_shifts_lane)
-// takes a prediction to about 1e-12, and a QR sweep with that shift all but
-// deflates its eigenvalue.  x and x' live in X and DX (n entries each).  A
-// step that is non-finite or longer than `maxstep` (the FP32 polish had not
-// converged there) leaves the prediction as it was; a zero subdiagonal (H
-// already splits) leaves all of them.
+// step takes a prediction to about 1e-12, and a QR sweep with that shift all
+// but deflates its eigenvalue.  Hyman's recurrence gives r(s) in FP64 (x in
+// X); the derivative r'(s) only has to be right to a few digits (Newton with
+// a derivative of relative error e gains a factor e on top of the quadratic
+// step), so its recurrence runs in FP32 on Hf, an FP32 copy of H (x' in DX):
+// half the step's FP64 work moves to the FP32 pipe.  x and x' are rescaled
+// together when x grows (the Newton ratio does not depend on their common
+// scale).  A step that is non-finite or longer than `maxstep` (the FP32 polish
+// had not converged there) leaves the prediction as it was; a zero
+// subdiagonal (H already splits) leaves all of them.
 template <class MH>
-__device__ void newton64_shifts_lane(const int n, const MH &H, const VecIlv<double> &S, const VecIlv<double> &X,
-                                     const VecIlv<double> &DX, const double maxstep)
+__device__ void newton64_shifts_lane(const int n, const MH &H, const MatIlv<float> &Hf, const VecIlv<double> &S,
+                                     const VecIlv<double> &X, const VecIlv<float> &DX, const double maxstep)
 {
     for (int i = 2; i <= n; ++i)
         if (H.ld(i, i - 1).r == 0.0) return;
     for (int k = 1; k <= n; ++k) {
         const cx<double> s = S.ld(k);
         if (nonfinite(s.r) || nonfinite(s.i)) continue;
+        const cx<float> sf = mk((float)s.r, (float)s.i);
         X.st(n, mk(1.0, 0.0));
-        DX.st(n, mk(0.0, 0.0));
+        DX.st(n, mk(0.f, 0.f));
         for (int i = n; i >= 2; --i) {
-            const cx<double> d = csub(H.ld(i, i), s);
             const cx<double> xi = X.ld(i);
-            cx<double> acc = cmul(d, xi);
-            cx<double> dacc = csub(cmul(d, DX.ld(i)), xi);
+            const cx<float> xif = mk((float)xi.r, (float)xi.i);
+            cx<double> acc = cmul(csub(H.ld(i, i), s), xi);
+            cx<float> dacc = csub(cmul(csub(Hf.ld(i, i), sf), DX.ld(i)), xif);
             for (int j = i + 1; j <= n; ++j) {
-                const cx<double> h = H.ld(i, j);
-                acc = cmac(acc, h, X.ld(j));
-                dacc = cmac(dacc, h, DX.ld(j));
+                acc = cmac(acc, H.ld(i, j), X.ld(j));
+                dacc = cmac(dacc, Hf.ld(i, j), DX.ld(j));
             }
             const double rs = -1.0 / H.ld(i, i - 1).r;
-            cx<double> xn = cscal(acc, rs), dxn = cscal(dacc, rs);
-            if (cabs1(xn) > 1e150) {  // rescale x, x' together (the Newton ratio is scale free)
+            cx<double> xn = cscal(acc, rs);
+            cx<float> dxn = cscal(dacc, (float)rs);
+            if (cabs1(xn) > 1e18) {
                 for (int j = i; j <= n; ++j) {
-                    X.st(j, cscal(X.ld(j), 1e-150));
-                    DX.st(j, cscal(DX.ld(j), 1e-150));
+                    X.st(j, cscal(X.ld(j), 1e-18));
+                    DX.st(j, cscal(DX.ld(j), 1e-18f));
                 }
-                xn = cscal(xn, 1e-150);
-                dxn = cscal(dxn, 1e-150);
+                xn = cscal(xn, 1e-18);
+                dxn = cscal(dxn, 1e-18f);
             }
             X.st(i - 1, xn);
             DX.st(i - 1, dxn);
         }
-        const cx<double> d1 = csub(H.ld(1, 1), s);
         const cx<double> x1 = X.ld(1);
-        cx<double> r = cmul(d1, x1);
-        cx<double> rp = csub(cmul(d1, DX.ld(1)), x1);
+        cx<double> r = cmul(csub(H.ld(1, 1), s), x1);
+        cx<float> rp = csub(cmul(csub(Hf.ld(1, 1), sf), DX.ld(1)), mk((float)x1.r, (float)x1.i));
         for (int j = 2; j <= n; ++j) {
-            const cx<double> h = H.ld(1, j);
-            r = cmac(r, h, X.ld(j));
-            rp = cmac(rp, h, DX.ld(j));
+            r = cmac(r, H.ld(1, j), X.ld(j));
+            rp = cmac(rp, Hf.ld(1, j), DX.ld(j));
         }
-        const cx<double> delta = cdiv(r, rp);
+        const cx<double> delta = cdiv(r, mk((double)rp.r, (double)rp.i));
         if (!nonfinite(delta.r) && !nonfinite(delta.i) && cabs1(delta) <= maxstep) S.st(k, csub(s, delta));
     }
 }

@@ -28,11 +28,11 @@ constexpr int kFusedThreads = 128;  // 4 warps per block
 
 // double2 elements per lane of one fused-kernel slot: H, Z (n^2 each), a work
 // vector (n); the shift-seeded kernel adds an FP32 copy of H (n^2 float2 =
-// ceil(n^2 / 2) double2) and the n predictions.
+// ceil(n^2 / 2) double2), the n predictions and an FP32 vector (n float2).
 __host__ __device__ __forceinline__ long long fused_slot_elems(int n, bool learned)
 {
     const long long nn = (long long)n * n;
-    return 2 * nn + n + (learned ? (nn + 1) / 2 + n : 0);
+    return 2 * nn + n + (learned ? (nn + 1) / 2 + n + (n + 1) / 2 : 0);
 }
 
 __device__ __forceinline__ long long soa_mat_off(long long m, int n, int tc)
@@ -122,18 +122,19 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
                 for (int k = 1; k <= n; ++k)
                     S.st(k, mk(a.rS[vo + (long long)(k - 1) * tc], a.iS[vo + (long long)(k - 1) * tc]));
             }
+            // FP32 copy of the Hessenberg matrix (for the in-kernel polish and the
+            // FP64 step's derivative): lane l's element e at float2 index e * 32 + l
+            // of the region after H, Z and the work vector
+            float2 *region = reinterpret_cast<float2 *>(base - lane + (2LL * n * n + n) * 32);
+            const MatIlv<float> Hf{region + lane, n};
+            if ((a.shift_polish > 0 || a.shift_newton64) && valid && !(status & ST_NONFINITE))
+                for (int j = 1; j <= n; ++j)
+                    for (int i = 1; i <= (j + 1 < n ? j + 1 : n); ++i) {
+                        const cx<double> h = H.ld(i, j);
+                        Hf.st(i, j, mk((float)h.r, (float)h.i));
+                    }
             if (a.shift_polish > 0) {
-                // FP32 copy of the Hessenberg matrix: lane l's element e at float2
-                // index e * 32 + l of the region after H, Z and the work vector
-                float2 *region = reinterpret_cast<float2 *>(base - lane + (2LL * n * n + n) * 32);
-                const MatIlv<float> Hf{region + lane, n};
                 const bool go = valid && !(status & ST_NONFINITE);
-                if (go)
-                    for (int j = 1; j <= n; ++j)
-                        for (int i = 1; i <= (j + 1 < n ? j + 1 : n); ++i) {
-                            const cx<double> h = H.ld(i, j);
-                            Hf.st(i, j, mk((float)h.r, (float)h.i));
-                        }
                 // stop below 1e-6 of the eigenvalue scale (FP32 resolution); keep
                 // a prediction whose last step was below 1e-3 of it
                 const float tol = (float)(1e-6 * scale), keep = (float)(1e-3 * scale), dup = (float)(1e-5 * scale);
@@ -147,9 +148,11 @@ __global__ void __launch_bounds__(kFusedThreads) fused_fp64_kernel(const FusedAr
                 }
             }
             if (a.shift_newton64 && valid && !(status & ST_NONFINITE) && n >= 2) {
-                // x in the work vector, x' where the FP32 copy of H was (n <= (n^2 + 1) / 2 entries)
-                const VecIlv<double> DX{base + (2LL * n * n + n) * 32};
-                for (int st = 0; st < a.shift_newton64; ++st) newton64_shifts_lane(n, H, S, W, DX, 1e-4 * scale);
+                // x in the work vector, x' (FP32) after the predictions
+                float2 *dregion = reinterpret_cast<float2 *>(
+                    base - lane + (2LL * n * n + n + ((long long)n * n + 1) / 2 + n) * 32);
+                const VecIlv<float> DX{dregion + lane};
+                for (int st = 0; st < a.shift_newton64; ++st) newton64_shifts_lane(n, H, Hf, S, W, DX, 1e-4 * scale);
             }
             sp.S = S;
             sp.n = n;
