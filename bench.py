@@ -29,7 +29,8 @@ roofline  the solver is FP64-pipe bound: achieved = algorithmic FP64 flops
 cpu_baseline  the oracle's C restatement of the reference CPU path (OpenMP,
         all host cores) on a bounded prefix of the same batch.
 forms   the other forms, each on its own batch, each verified (residuals on the
-        device; learned: eigenvalues against the plain solve):
+        device; FP32+refine and learned: eigenvalues against the plain FP64 solve of
+        the same batch, max and median per-matrix error relative to ||A||_F):
         FP32+refine  n=16 (the same batch) and n=32 (262,144 Gaussian, seed 3,
                      beside plain FP64 on the same batch);
         learned shift  n=16 and n=32 on the family A0 + p1 A1 + p2 A2 + p3 A3
@@ -302,8 +303,10 @@ def device_residual_check(dAr, dAi, dEr, dEi, dVr, dVi, n, tc, chunk=1 << 17):
 
 def measure_form(name, n, N, seed, tc, precision, warmup, steps):
     """Device-resident eigensolves/s of one form on one seeded Gaussian batch,
-    verified on the device afterwards (every residual).  Returns the compact
-    entry of the JSON line and the detail record (stderr)."""
+    verified on the device afterwards (every residual; for FP32+refine also the
+    eigenvalues against a plain FP64 solve of the same batch: max and median over
+    the matrices of each matrix's largest distance, relative to ||A||_F).
+    Returns the compact entry of the JSON line and the detail record (stderr)."""
     import torch
     import ves
     import workloads
@@ -361,6 +364,15 @@ def measure_form(name, n, N, seed, tc, precision, warmup, steps):
         out["fb"] = fb
         detail.update(fp64_fallback_matrices=fb, fp64_residuals=res64, fp32_corrections=corr32,
                       ff_residuals=resff, fp64_residuals_per_pair=res64 / max(1, (N - fb) * n))
+        # eigenvalues against the plain FP64 solve of the same batch (untimed)
+        dE0r, dE0i = torch.empty_like(dEr), torch.empty_like(dEi)
+        ves.eigensolve(n, bc, tc, dAr, dAi, dE0r, dE0i, dVr, dVi, stream=stream)
+        torch.cuda.synchronize()
+        emax, emed = eig_errors(_vec(dEr, dEi, n, tc), _vec(dE0r, dE0i, n, tc), _mat(dAr, dAi, n, tc))
+        out["eig_err"] = r4(emax)
+        out["passed"] = passed and emax <= 1e-12
+        detail.update(eig_err_vs_fp64_max=emax, eig_err_vs_fp64_median=emed)
+        del dE0r, dE0i
     del dAr, dAi, dEr, dEi, dVr, dVi, wsp
     torch.cuda.empty_cache()
     return out, detail
@@ -375,6 +387,18 @@ def _mat(re, im, n, tc):
 def _vec(re, im, n, tc):
     import torch
     return torch.complex(re.view(-1, n, tc).permute(0, 2, 1), im.view(-1, n, tc).permute(0, 2, 1)).reshape(-1, n)
+
+
+def eig_errors(E1, E0, A, chunk=1 << 16):
+    """Per matrix, the largest distance from an eigenvalue in E1 to the nearest one
+    in E0, relative to ||A||_F; returns its max and median over the matrices (device)."""
+    import torch
+    per = []
+    for s in range(0, E1.shape[0], chunk):
+        d = (E1[s:s + chunk, :, None] - E0[s:s + chunk, None, :]).abs().amin(dim=2).amax(dim=1)
+        per.append(d / torch.linalg.matrix_norm(A[s:s + chunk]))
+    per = torch.cat(per)
+    return float(per.max()), float(per.median())
 
 
 def eig_distance(E1, E0, A, chunk=1 << 17):
